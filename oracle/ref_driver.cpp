@@ -1,0 +1,156 @@
+/*
+ * ref_driver.cpp -- drives bricklib's own CPU brick path, compiled from the
+ * reference's headers where they lie (see oracle/Makefile, target `ref`).
+ *
+ * TEST INFRASTRUCTURE ONLY: it produces golden vectors and pins the C
+ * restatement in brick_oracle.c.  Nothing in the product links it.
+ *
+ * What it runs is the reference's single-node CPU path of stencils/3axis.cpp
+ * d3pt7() (:14-92), generalised to a runtime tap list:
+ *   init_grid<3>            include/bricksetup.h:73-90
+ *   BrickStorage::allocate  include/brick.h:68-75 (bIn / bOut interleaved, 3axis.cpp:26-28)
+ *   copyToBrick<3>          include/bricksetup.h:172-181
+ *   accessor brick kernel   3axis.cpp:51-66 (bOut[b][k][j][i] = sum c * bIn[b][k+dk][j+dj][i+di])
+ *   array kernel            3axis.cpp:32-37 (_TILEFOR over the ghost-inclusive region)
+ *   compareBrick<3>         include/brickcompare.h:30-57 (tolerance 1e-6, cmpconst.h:7)
+ *   copyFromBrick<3>        include/bricksetup.h:213-221
+ * The generated-code kernels (brick("x.py", ...)) need the vecscatter code generator at
+ * build time and are not built here.
+ */
+#include <cstring>
+#include <vector>
+
+#include "brick.h"
+#include "bricksetup.h"
+#include "brickcompare.h"
+
+namespace {
+
+constexpr long GZ = 8;       // ghost zone, elements (stencils.h:14)
+constexpr long PADDING = 8;  // array padding, elements (stencils.h:15)
+
+template <unsigned BK, unsigned BJ, unsigned BI, typename Fold>
+struct Lay {
+  typedef Brick<Dim<BK, BJ, BI>, Fold> B;
+  static constexpr unsigned bk = BK, bj = BJ, bi = BI;
+};
+
+template <typename L>
+void offsets(long *out) {
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<3>(grid_ptr, {1, 1, 1});
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, L::B::BRICKSIZE);
+  typename L::B br(&bInfo, bStorage, 0);
+  for (unsigned k = 0; k < L::bk; ++k)
+    for (unsigned j = 0; j < L::bj; ++j)
+      for (unsigned i = 0; i < L::bi; ++i)
+        out[(k * L::bj + j) * L::bi + i] = (long)(&br[0][k][j][i] - br.dat);
+  free(grid_ptr);
+  free(bInfo.adj);
+}
+
+template <typename L>
+int sweep(long n, const double *in_arr, int npts, const int *offs, const double *coeff,
+          double *out_brick, double *out_arr) {
+  const long STRIDE = n + 2 * (GZ + PADDING), STRIDEG = n + 2 * GZ;
+  const long gk = STRIDEG / L::bk, gj = STRIDEG / L::bj, gi = STRIDEG / L::bi;
+  const long sz = STRIDE * STRIDE * STRIDE;
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<3>(grid_ptr, {gi, gj, gk});
+  const unsigned bsize = L::B::BRICKSIZE;
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, bsize * 2);
+  typename L::B bIn(&bInfo, bStorage, 0);
+  typename L::B bOut(&bInfo, bStorage, bsize);
+  std::memset(bStorage.dat.get(), 0, sizeof(bElem) * bStorage.chunks * bStorage.step);
+
+  bElem *in_ptr = (bElem *)aligned_alloc(ALIGN, sizeof(bElem) * sz);
+  std::memcpy(in_ptr, in_arr, sizeof(bElem) * sz);
+  copyToBrick<3>({STRIDEG, STRIDEG, STRIDEG}, {PADDING, PADDING, PADDING}, {0, 0, 0}, in_ptr, grid_ptr, bIn);
+
+  // array kernel, ghost-inclusive region like _TILEFOR (stencils.h:28-35)
+  std::memset(out_arr, 0, sizeof(bElem) * sz);
+  for (long k = PADDING; k < PADDING + STRIDEG; ++k)
+    for (long j = PADDING; j < PADDING + STRIDEG; ++j)
+      for (long i = PADDING; i < PADDING + STRIDEG; ++i) {
+        bElem v = coeff[0] * in_ptr[((k + offs[0]) * STRIDE + j + offs[1]) * STRIDE + i + offs[2]];
+        for (int t = 1; t < npts; ++t)
+          v = v + coeff[t] * in_ptr[((k + offs[3 * t]) * STRIDE + j + offs[3 * t + 1]) * STRIDE + i + offs[3 * t + 2]];
+        out_arr[(k * STRIDE + j) * STRIDE + i] = v;
+      }
+
+  // accessor brick kernel over interior bricks (3axis.cpp:51-66)
+  auto grid = grid_ptr;
+  for (long tk = GZ / L::bk; tk < gk - GZ / L::bk; ++tk)
+    for (long tj = GZ / L::bj; tj < gj - GZ / L::bj; ++tj)
+      for (long ti = GZ / L::bi; ti < gi - GZ / L::bi; ++ti) {
+        unsigned b = grid[(tk * gj + tj) * gi + ti];
+        for (long k = 0; k < L::bk; ++k)
+          for (long j = 0; j < L::bj; ++j)
+            for (long i = 0; i < L::bi; ++i) {
+              bElem v = coeff[0] * bIn[b][k + offs[0]][j + offs[1]][i + offs[2]];
+              for (int t = 1; t < npts; ++t)
+                v = v + coeff[t] * bIn[b][k + offs[3 * t]][j + offs[3 * t + 1]][i + offs[3 * t + 2]];
+              bOut[b][k][j][i] = v;
+            }
+      }
+
+  bool ok = compareBrick<3>({n, n, n}, {PADDING, PADDING, PADDING}, {GZ, GZ, GZ}, out_arr, grid_ptr, bOut);
+  std::memset(out_brick, 0, sizeof(bElem) * sz);
+  copyFromBrick<3>({n, n, n}, {PADDING, PADDING, PADDING}, {GZ, GZ, GZ}, out_brick, grid_ptr, bOut);
+
+  free(in_ptr);
+  free(grid_ptr);
+  free(bInfo.adj);
+  return ok ? 1 : 0;
+}
+
+typedef Lay<8, 8, 8, Dim<4, 8>> L0;     // CUDA fold (stencils/cudavfold.h:9)
+typedef Lay<8, 8, 8, Dim<8>> L1;        // AVX-512 fold (stencils/cpuvfold.h:12-13)
+typedef Lay<8, 8, 8, Dim<2, 2>> L2;     // docs/usingbricks.md example fold
+typedef Lay<8, 8, 8, Dim<2, 4, 4>> L3;  // three-level fold
+typedef Lay<4, 4, 4, Dim<4, 4>> L4;     // 4^3 bricks
+typedef Lay<16, 8, 8, Dim<4, 8>> L5;    // 16x8x8 bricks
+typedef Lay<8, 8, 32, Dim<4, 8>> L6;    // 8x8x32 bricks
+
+}  // namespace
+
+extern "C" {
+
+/* Layout ids: 0 (8,8,8)/(4,8)  1 (8,8,8)/(8)  2 (8,8,8)/(2,2)  3 (8,8,8)/(2,4,4)
+ *             4 (4,4,4)/(4,4)  5 (16,8,8)/(4,8)  6 (8,8,32)/(4,8) */
+int ref_layout_offsets(int layout, long *out) {
+  switch (layout) {
+    case 0: offsets<L0>(out); return 0;
+    case 1: offsets<L1>(out); return 0;
+    case 2: offsets<L2>(out); return 0;
+    case 3: offsets<L3>(out); return 0;
+    case 4: offsets<L4>(out); return 0;
+    case 5: offsets<L5>(out); return 0;
+    case 6: offsets<L6>(out); return 0;
+  }
+  return -1;
+}
+
+int ref_init_grid(long gk, long gj, long gi, unsigned *grid, unsigned *adj) {
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<3>(grid_ptr, {gi, gj, gk});
+  std::memcpy(grid, grid_ptr, sizeof(unsigned) * gk * gj * gi);
+  std::memcpy(adj, bInfo.adj, sizeof(unsigned) * 27 * bInfo.nbricks);
+  free(grid_ptr);
+  free(bInfo.adj);
+  return 0;
+}
+
+/* One sweep on an n^3 interior with an 8-cell ghost zone and 8-cell array padding.
+ * in_arr, out_brick, out_arr: (n+32)^3 arrays.  Returns 1 when compareBrick matches. */
+int ref_sweep(int layout, long n, const double *in_arr, int npts, const int *offs, const double *coeff,
+              double *out_brick, double *out_arr) {
+  switch (layout) {
+    case 0: return sweep<L0>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
+    case 1: return sweep<L1>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
+    case 4: return sweep<L4>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
+  }
+  return -1;
+}
+
+}  // extern "C"

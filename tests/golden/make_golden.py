@@ -1,0 +1,85 @@
+"""Generate the golden fixtures in this directory from bricklib's own CPU brick
+path (oracle/_ref/libbrickref.so, compiled from the reference sources by
+`make -C oracle ref`).  Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+Fixtures written:
+  layouts.npz       in-brick element offsets computed by the reference accessor
+                    (include/brick.h:213-327) for seven brick-dims / vector-fold pairs
+  init_grid.npz     grid and adjacency of init_grid<3> (include/bricksetup.h:73-90) on 5x4x3
+  sweep_<shape>.npz one sweep on a 16^3 interior (+8 ghost, +8 padding) through
+                    copyToBrick -> accessor brick kernel -> compareBrick -> copyFromBrick,
+                    input uniform[-1,1) from splitmix64 seed 1234: the interior output,
+                    the max |brick - array| difference and the reference's compareBrick verdict
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+from bricklib_gb300 import stencils  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+LAYOUTS = {  # id: (bdim k,j,i ; fold k,j,i)
+    0: ((8, 8, 8), (1, 4, 8)),
+    1: ((8, 8, 8), (1, 1, 8)),
+    2: ((8, 8, 8), (1, 2, 2)),
+    3: ((8, 8, 8), (2, 4, 4)),
+    4: ((4, 4, 4), (1, 4, 4)),
+    5: ((16, 8, 8), (1, 4, 8)),
+    6: ((8, 8, 32), (1, 4, 8)),
+}
+
+N = 16
+SEED_IN = 1234
+SEED_COEFF = 99
+
+
+def main():
+    oracle.build()
+    R = oracle.ref()
+    if R is None:
+        raise SystemExit("reference checker not built (needs the reference tree)")
+
+    lay = {}
+    for lid, (bdim, fold) in LAYOUTS.items():
+        out = np.zeros(int(np.prod(bdim)), dtype=np.int64)
+        assert R.ref_layout_offsets(lid, out) == 0
+        lay[f"offsets_{lid}"] = out
+        lay[f"bdim_{lid}"] = np.asarray(bdim)
+        lay[f"fold_{lid}"] = np.asarray(fold)
+    np.savez(os.path.join(OUT, "layouts.npz"), **lay)
+
+    gk, gj, gi = 3, 4, 5
+    grid = np.zeros(gk * gj * gi, dtype=np.uint32)
+    adj = np.zeros(gk * gj * gi * 27, dtype=np.uint32)
+    R.ref_init_grid(gk, gj, gi, grid, adj)
+    np.savez(os.path.join(OUT, "init_grid.npz"), grid=grid, adj=adj, dims=np.asarray([gk, gj, gi]))
+
+    S = N + 32
+    inp = stencils.uniform(SEED_IN, S * S * S)
+    cases = [(name, 0) for name in stencils.PLAIN_SHAPES] + [("heat7", 0), ("lap7", 0), ("star7", 4)]
+    for name, lid in cases:
+        st = stencils.make(name, SEED_COEFF)
+        offs = st.offsets().reshape(-1).astype(np.int32)
+        ob = np.zeros(S * S * S)
+        oa = np.zeros(S * S * S)
+        ok = R.ref_sweep(lid, N, inp, st.npoints, offs, st.coeff, ob, oa)
+        assert ok in (0, 1)
+        ob = ob.reshape(S, S, S)[16:16 + N, 16:16 + N, 16:16 + N].copy()
+        oa = oa.reshape(S, S, S)[16:16 + N, 16:16 + N, 16:16 + N].copy()
+        tag = name if lid == 0 else f"{name}_layout{lid}"
+        np.savez(os.path.join(OUT, f"sweep_{tag}.npz"), out=ob, arr_maxdiff=np.max(np.abs(ob - oa)),
+                 ref_match=ok, n=N, seed_in=SEED_IN, seed_coeff=SEED_COEFF, layout=lid,
+                 offsets=st.offsets(), coeff=st.coeff, input_sum=inp.sum())
+        print(f"{tag:22s} compareBrick={ok} max|brick-array|={np.max(np.abs(ob - oa)):.3e}")
+
+
+if __name__ == "__main__":
+    main()
