@@ -1,0 +1,370 @@
+"""Benchmark of the brick stencil sweep on one GB300 (or N independent replicas).
+
+Workload (default): the plain FP64 drop-in at 512^3 interior + an 8-cell ghost zone,
+8x8x8 bricks with the CUDA vector fold (4,8), one sweep each of the 7-point star (r=1),
+13-point star (r=2), 25-point star (r=4), 27-point cube (r=1) and 125-point cube (r=2),
+seeded uniform[-1,1) input and seeded coefficients normalised to sum 1.  One step = one
+sweep of every shape.  GStencil/s = interior points x sweeps / seconds (the reference's
+tot_elems * 1e-9 / time, weak/main.cu:315-317).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun every rank runs the same workload on its own GPU (replicas: the sweep
+has no exchange step on one node); the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPES = ("star7", "star13", "star25", "cube27", "cube125")
+SEED_IN, SEED_COEFF = 20261203, 7
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_PATH = os.path.join(ROOT, "profiles", "traffic.json")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=512)
+    p.add_argument("--dtype", default="f64", choices=["f64", "f32", "bf16"])
+    p.add_argument("--acc", default="native", choices=["native", "compensated", "floatfloat"])
+    p.add_argument("--shapes", default=",".join(SHAPES))
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_table():
+    try:
+        with open(TRAFFIC_PATH) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.device)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import torch
+    from bricklib_gb300 import _abi, bricks as B, stencils
+    from bricklib_gb300._abi import call
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    call("bk_set_device", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    dtype = B.DTYPE_NAMES[args.dtype]
+    acc = {"native": _abi.BK_ACC_NATIVE, "compensated": _abi.BK_ACC_COMPENSATED,
+           "floatfloat": _abi.BK_ACC_FLOATFLOAT}[args.acc]
+    esize = B.ELEM_SIZE[dtype]
+    shapes = args.shapes.split(",")
+
+    n = args.n
+    lay = B.DEFAULT_LAYOUT
+    g = (n + 16) // 8
+    grid, info = B.init_grid([g, g, g])
+    nbricks = info.nbricks
+    g3 = grid.reshape(g, g, g)
+    interior = np.ascontiguousarray(g3[1:-1, 1:-1, 1:-1].reshape(-1))
+    dinfo = B.movBrickInfo(info)
+    blist = B.BrickList(interior)
+    bsize = lay.size
+    s_in = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
+    s_out = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
+    b_in, b_out = B.Brick(dinfo, s_in, 0, lay), B.Brick(dinfo, s_out, 0, lay)
+    call("bk_fill_uniform", C.c_void_p(s_in.ptr), nbricks * bsize, dtype, SEED_IN, -1.0, 1.0, sp)
+    sts = {name: stencils.make(name, SEED_COEFF) for name in shapes}
+    csts = {name: B.to_c_stencil(st) for name, st in sts.items()}
+    points = n ** 3
+
+    def sweep(name):
+        B.brickSweep(b_in, b_out, blist, csts[name], acc, stream=sp)
+
+    # warm-up
+    for _ in range(args.warmup):
+        for name in shapes:
+            sweep(name)
+    torch.cuda.synchronize()
+    if B.error_flags(sp) != 0:
+        raise RuntimeError("device error flags raised during warm-up")
+
+    K = args.steps
+    ev = {name: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+          for name in shapes}
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0.record(stream)
+        for k in range(K):
+            for name in shapes:
+                ev[name][k][0].record(stream)
+                sweep(name)
+                ev[name][k][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    total_ms = t0.elapsed_time(t1)
+    if ws > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    per_shape_ms = {name: sum(a.elapsed_time(b) for a, b in ev[name]) / K for name in shapes}
+    ms_per_step = total_ms / K
+    value = ws * len(shapes) * points / (ms_per_step * 1e-3) / 1e9
+
+    hbm, peak_kind = peaks()
+    fp64_rate = C.c_double()
+    call("bk_measure_fma_rate", _abi.BK_F64 if dtype == _abi.BK_F64 else _abi.BK_F32, sp, C.byref(fp64_rate))
+    bytes_pt = 2 * esize
+    per_shape = {}
+    for name in shapes:
+        ms = per_shape_ms[name]
+        gst = points / (ms * 1e-3) / 1e9
+        flops = sts[name].flops_per_point * points / (ms * 1e-3)
+        per_shape[name] = {"ms": round(ms, 4), "gstencil_s": round(gst, 2),
+                           "hbm_frac": round(gst * 1e9 * bytes_pt / (hbm * 1e9), 4),
+                           "compute_frac": round(flops / fp64_rate.value, 4)}
+    dom = max(shapes, key=lambda s: per_shape_ms[s])
+    dom_ms = per_shape_ms[dom]
+    achieved = points * bytes_pt / (dom_ms * 1e-3) / 1e9
+    tr = traffic_table().get(f"{args.dtype}:{args.acc}:{dom}:{n}")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": tr, "kernel": f"sweep_kernel {dom}",
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "compute": {"unit": "TFLOP/s", "achieved": round(sts[dom].flops_per_point * points / (dom_ms * 1e-3) / 1e12, 3),
+                            "peak": round(fp64_rate.value / 1e12, 3),
+                            "peak_source": f"measured {'FP64' if dtype == _abi.BK_F64 else 'FP32'} FMA rate (bk_measure_fma_rate)"}}
+
+    # end to end through the public API: pinned host input -> device, sweeps, results -> host
+    e2e = None
+    if not args.no_e2e:
+        nbytes = nbricks * bsize * esize
+        h_in, h_out = B.PinnedBuffer(nbytes), B.PinnedBuffer(nbytes)
+        B.memcpy(h_in.ptr, s_in.ptr, nbytes, 1, sp)
+        torch.cuda.synchronize()
+        Ke = max(1, min(K, 5))
+        for it in range(Ke + 1):
+            if it == 1:
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            B.memcpy(s_in.ptr, h_in.ptr, nbytes, 0, sp)
+            for name in shapes:
+                sweep(name)
+                B.memcpy(h_out.ptr, s_out.ptr, nbytes, 1, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e_ms = e0.elapsed_time(e1) / Ke
+        e2e = {"value": round(ws * len(shapes) * points / (e_ms * 1e-3) / 1e9, 3), "unit": "GStencil/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3)}
+
+    # CPU baseline: the oracle's OpenMP brick sweep on a sample of the same bricks,
+    # also used as a spot check of the GPU output on those bricks
+    cpu = None
+    if not args.no_cpu and rank == 0 and dtype == _abi.BK_F64:
+        cpu = cpu_baseline_on_device_data(B, s_in, s_out, info, interior, sts, shapes, lay, nbricks, bsize, sp,
+                                          lambda name: (sweep(name), torch.cuda.synchronize()))
+
+    if rank == 0:
+        line = {"metric": "GStencil/s", "value": round(value, 3), "unit": "GStencil/s", "n_gpus": ws,
+                "steps": K, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": {"f64": "f64", "f32": "f32", "bf16": "bf16"}[args.dtype],
+                "data": "synthetic: seeded uniform[-1,1) input, seeded coefficients normalised to sum 1",
+                "config": {"workload": f"plain {args.dtype} brick sweep, {n}^3 interior + 8-cell ghost, 8x8x8 bricks "
+                                       f"fold (4,8), one sweep each of {'/'.join(shapes)}",
+                           "interior_points": points, "bricks": nbricks, "accumulation": args.acc,
+                           "l2": f"no flush: inputs {nbricks * bsize * esize / 1e9:.2f} GB per field > 129 MB L2",
+                           "parallelism": f"replicas x{ws}"},
+                "per_stencil": per_shape, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": K * len(shapes), "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_on_device_data(B, s_in, s_out, info, interior, sts, shapes, lay, nbricks, bsize, sp, run_one):
+    from oracle import oracle
+    host_in = np.empty(nbricks * bsize, dtype=np.float64)
+    B.memcpy(host_in.ctypes.data, s_in.ptr, host_in.nbytes, 1, sp)
+    B.synchronize(sp)
+    adj = np.ascontiguousarray(info.adj.reshape(-1))
+    threads = oracle.max_threads()
+    rng = np.random.default_rng(1)
+    res = {}
+    total_pts, total_s = 0, 0.0
+    max_err = 0.0
+    for name in shapes:
+        st = sts[name]
+        # ~2 s of CPU work per shape at the expected rate
+        rate = 2e9 / st.flops_per_point * threads / 8  # points/s guess
+        m = int(min(len(interior), max(64, 2.0 * rate / bsize)))
+        sample = np.ascontiguousarray(np.sort(rng.choice(interior, size=m, replace=False)), dtype=np.uint32)
+        out = np.zeros(nbricks * bsize, dtype=np.float64)
+        t = time.perf_counter()
+        oracle.brick_sweep(adj, host_in, bsize, 0, out, bsize, 0, sample, lay.bdim, lay.fold, st.offsets(), st.coeff,
+                           threads)
+        dt = time.perf_counter() - t
+        total_pts += m * bsize
+        total_s += dt
+        res[name] = round(m * bsize / dt / 1e9, 4)
+        # spot check against the GPU result for the same bricks
+        run_one(name)
+        gpu = np.empty(nbricks * bsize, dtype=np.float64)
+        B.memcpy(gpu.ctypes.data, s_out.ptr, gpu.nbytes, 1, sp)
+        B.synchronize(sp)
+        idx = (sample[:, None].astype(np.int64) * bsize + np.arange(bsize)[None, :]).reshape(-1)
+        a, b = gpu[idx], out[idx]
+        max_err = max(max_err, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+    return {"value": round(total_pts / total_s / 1e9, 4), "unit": "GStencil/s", "cores": threads, "kind": "port",
+            "sample": f"oracle OpenMP brick sweep on a random sample of interior bricks per shape "
+                      f"(~2 s each), {total_pts} points in {total_s:.1f} s",
+            "per_stencil": res, "gpu_vs_oracle_max_normwise_err": max_err}
+
+
+# ---------------------------------------------------------------------------- reference arm
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from bricklib_gb300 import stencils
+    from oracle import oracle
+    oracle.build()
+    shapes = args.shapes.split(",")
+    # the reference's CPU brick path, timed on a 64^3-interior sample of the workload per
+    # shape per step (same bricks, fold and taps; the reference-compiled build does not
+    # travel to an aarch64 host, so the OpenMP restatement of it runs here)
+    m = 64
+    dom = oracle.Domain(m)
+    arr = stencils.uniform(SEED_IN, int(np.prod(dom.adims))).reshape(dom.adims)
+    dat = dom.alloc()
+    dom.to_bricks(arr, dat, 0)
+    threads = oracle.max_threads()
+    sts = {name: stencils.make(name, SEED_COEFF) for name in shapes}
+
+    def step():
+        for name in shapes:
+            st = sts[name]
+            oracle.brick_sweep(dom.adj, dat, dom.step, 0, dat, dom.step, dom.bsize, dom.interior, dom.bdim, dom.fold,
+                               st.offsets(), st.coeff, threads)
+
+    for _ in range(args.warmup):
+        step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t) / args.steps
+    value = len(shapes) * m ** 3 / dt / 1e9
+    line = {"impl": "reference", "metric": "GStencil/s", "value": round(value, 4), "unit": "GStencil/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded uniform[-1,1) input, seeded coefficients normalised to sum 1",
+            "config": {"workload": f"plain f64 brick sweep, {args.n}^3 interior + 8-cell ghost, 8x8x8 bricks, "
+                                   f"one sweep each of {'/'.join(shapes)}",
+                       "sample": f"{m}^3 interior per shape per step"},
+            "cpu_baseline": {"value": round(value, 4), "unit": "GStencil/s", "cores": threads, "kind": "port",
+                             "sample": f"{m}^3 interior (+ghost) per shape per step, OpenMP brick sweep of the oracle"},
+            "e2e": {"value": round(value, 4), "unit": "GStencil/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -1,0 +1,257 @@
+// The brick stencil sweep kernel (templated; instantiated per element type in
+// sweep_f64.cu / sweep_f32.cu / sweep_bf16.cu).
+//
+// One CTA computes NB bricks at a time (NB = threads / (BJ*BI)).  For each brick it
+//   1. reads the brick's 27 adjacency entries (BrickInfo::adj, brick.h:96-111) into
+//      shared memory, clamping out-of-range indices to brick 0 and raising a flag;
+//   2. gathers the extended tile (BK+2R) x (BJ+2R) x (BI+2R) from the centre brick
+//      and its neighbours into shared memory in row-major order, converting from the
+//      storage type to the accumulation type once per element (star stencils skip
+//      the edge and corner regions they never read);
+//   3. lets each thread compute one (j, i) column of BK outputs from shared memory
+//      and store it, coalesced, into the output field of brick adj[b][13].
+// The tap structure is compile-time for the star / cube families and a runtime list
+// (offsets into the tile, coefficients in the parameter constant bank) for the
+// generic family.
+#pragma once
+
+#include "bk_common.cuh"
+
+namespace bk {
+
+enum Family { FAM_GENERIC = 0, FAM_STAR = 1, FAM_CUBE = 2 };
+enum AccMode { ACCM_NATIVE = 0, ACCM_COMP = 1 };
+
+struct SweepArgs {
+  const unsigned *adj;
+  unsigned nbricks;
+  const void *in;
+  unsigned long long in_step, in_off;
+  long long in_chunks;
+  void *out;
+  unsigned long long out_step, out_off;
+  long long out_chunks;
+  const unsigned *blist;
+  unsigned nlist;
+  int *err;
+  Layout L;
+};
+
+// Coefficients in kernel order; passed by value (kernel parameter constant bank).
+struct Taps {
+  int n;
+  int toff[BK_MAX_TAPS];  // generic family: tap offset in tile elements from the centre
+  float cf[BK_MAX_TAPS];
+  double c[BK_MAX_TAPS];
+};
+
+__host__ __device__ constexpr int sweep_threads(int tpb) { return tpb < 128 ? 128 : tpb; }
+
+template <typename AT> __device__ __forceinline__ AT coef(const Taps &tp, int t);
+template <> __device__ __forceinline__ double coef<double>(const Taps &tp, int t) { return tp.c[t]; }
+template <> __device__ __forceinline__ float coef<float>(const Taps &tp, int t) { return tp.cf[t]; }
+
+// Neumaier compensated accumulation of one partial into (s, comp).
+__device__ __forceinline__ double absval(double x) { return fabs(x); }
+__device__ __forceinline__ float absval(float x) { return fabsf(x); }
+
+template <typename AT>
+__device__ __forceinline__ void neumaier(AT &s, AT &comp, AT p) {
+  const AT t = s + p;
+  comp += (absval(s) >= absval(p)) ? ((s - t) + p) : ((p - t) + s);
+  s = t;
+}
+
+// One output point; c points at the centre element in the tile.
+template <typename AT, int EJ, int EI, int R, int FAM, int ACC>
+__device__ __forceinline__ AT stencil_point(const AT *__restrict__ c, const Taps &tp) {
+  constexpr int SJ = EI, SK = EJ * EI;
+  if (FAM == FAM_STAR) {
+    if (ACC == ACCM_NATIVE) {
+      AT v = coef<AT>(tp, 0) * c[0];
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1);
+        v = fma(coef<AT>(tp, t + 0), c[d], v);
+        v = fma(coef<AT>(tp, t + 1), c[-d], v);
+        v = fma(coef<AT>(tp, t + 2), c[d * SJ], v);
+        v = fma(coef<AT>(tp, t + 3), c[-d * SJ], v);
+        v = fma(coef<AT>(tp, t + 4), c[d * SK], v);
+        v = fma(coef<AT>(tp, t + 5), c[-d * SK], v);
+      }
+      return v;
+    } else {
+      // partial 0: the i row (centre and i taps) as an FMA chain; every j / k tap is
+      // its own partial; partials are combined with Neumaier's compensated sum
+      AT row = coef<AT>(tp, 0) * c[0];
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1);
+        row = fma(coef<AT>(tp, t + 0), c[d], row);
+        row = fma(coef<AT>(tp, t + 1), c[-d], row);
+      }
+      AT s = row, comp = AT(0);
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1);
+        neumaier(s, comp, coef<AT>(tp, t + 2) * c[d * SJ]);
+        neumaier(s, comp, coef<AT>(tp, t + 3) * c[-d * SJ]);
+        neumaier(s, comp, coef<AT>(tp, t + 4) * c[d * SK]);
+        neumaier(s, comp, coef<AT>(tp, t + 5) * c[-d * SK]);
+      }
+      return s + comp;
+    }
+  } else if (FAM == FAM_CUBE) {
+    if (ACC == ACCM_NATIVE) {
+      AT v = AT(0);
+#pragma unroll
+      for (int dk = -R; dk <= R; ++dk)
+#pragma unroll
+        for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+          for (int di = -R; di <= R; ++di) {
+            const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+            const AT x = c[dk * SK + dj * SJ + di];
+            v = (t == 0) ? coef<AT>(tp, 0) * x : fma(coef<AT>(tp, t), x, v);
+          }
+      return v;
+    } else {
+      // each (dk, dj) row of 2R+1 taps is an FMA chain; rows are Neumaier-summed
+      AT s = AT(0), comp = AT(0);
+#pragma unroll
+      for (int dk = -R; dk <= R; ++dk)
+#pragma unroll
+        for (int dj = -R; dj <= R; ++dj) {
+          const int t0 = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1);
+          AT row = coef<AT>(tp, t0) * c[dk * SK + dj * SJ - R];
+#pragma unroll
+          for (int di = -R + 1; di <= R; ++di)
+            row = fma(coef<AT>(tp, t0 + di + R), c[dk * SK + dj * SJ + di], row);
+          if (dk == -R && dj == -R) s = row;
+          else neumaier(s, comp, row);
+        }
+      return s + comp;
+    }
+  } else {
+    if (ACC == ACCM_NATIVE) {
+      AT v = coef<AT>(tp, 0) * c[tp.toff[0]];
+      for (int t = 1; t < tp.n; ++t) v = fma(coef<AT>(tp, t), c[tp.toff[t]], v);
+      return v;
+    } else {
+      AT s = coef<AT>(tp, 0) * c[tp.toff[0]], comp = AT(0);
+      for (int t = 1; t < tp.n; ++t) neumaier(s, comp, coef<AT>(tp, t) * c[tp.toff[t]]);
+      return s + comp;
+    }
+  }
+}
+
+template <typename T, int BK, int BJ, int BI, int R, int FAM, bool RM, int ACC>
+__global__ void __launch_bounds__(sweep_threads(BJ * BI))
+sweep_kernel(const SweepArgs a, const Taps tp) {
+  typedef typename Elem<T>::acc AT;
+  constexpr int TPB = BJ * BI;
+  constexpr int NT = sweep_threads(TPB);
+  constexpr int NB = NT / TPB;
+  constexpr int EK = BK + 2 * R, EJ = BJ + 2 * R, EI = BI + 2 * R;
+  constexpr int TILE = EK * EJ * EI;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  AT *tiles = reinterpret_cast<AT *>(smem_raw);
+  unsigned *nbrs = reinterpret_cast<unsigned *>(smem_raw + sizeof(AT) * TILE * NB);
+
+  const int slot = threadIdx.x / TPB, lt = threadIdx.x % TPB;
+  AT *tile = tiles + slot * TILE;
+  unsigned *nbr = nbrs + slot * 28;
+  const T *in = reinterpret_cast<const T *>(a.in) + a.in_off;
+  T *out = reinterpret_cast<T *>(a.out) + a.out_off;
+
+  for (long long base = (long long)blockIdx.x * NB; base < a.nlist; base += (long long)gridDim.x * NB) {
+    const long long n = base + slot;
+    if (lt < 27) {
+      unsigned v = 0;
+      int ok = 0;
+      if (n < a.nlist) {
+        const unsigned b = a.blist[n];
+        if (b < a.nbricks) {
+          v = a.adj[(size_t)b * 27 + lt];
+          ok = 1;
+          // the centre entry is also the output brick: out of range skips the brick
+          if (lt == 13 && ((long long)v >= a.out_chunks || (long long)v >= a.in_chunks)) ok = 0;
+          if ((long long)v >= a.in_chunks || !ok) { atomicOr(a.err, FLAG_BOUNDS); v = 0; }
+        } else if (lt == 13) {
+          atomicOr(a.err, FLAG_BOUNDS);
+        }
+      }
+      nbr[lt] = v;
+      if (lt == 13) nbr[27] = ok;
+    }
+    __syncthreads();
+    const bool active = nbr[27] != 0;
+    if (active) {
+      for (int e = lt; e < TILE; e += TPB) {
+        const int kk = e / (EJ * EI), rem = e - kk * (EJ * EI);
+        const int jj = rem / EI, ii = rem - jj * EI;
+        const int qk = kk < R ? -1 : (kk >= R + BK ? 1 : 0);
+        const int qj = jj < R ? -1 : (jj >= R + BJ ? 1 : 0);
+        const int qi = ii < R ? -1 : (ii >= R + BI ? 1 : 0);
+        if (FAM == FAM_STAR && ((qk != 0) + (qj != 0) + (qi != 0)) > 1) continue;
+        const int lk = kk - R - qk * BK, lj = jj - R - qj * BJ, li = ii - R - qi * BI;
+        const unsigned nb = nbr[(qk + 1) * 9 + (qj + 1) * 3 + (qi + 1)];
+        const int o = RM ? (lk * BJ + lj) * BI + li : a.L.offset(lk, lj, li);
+        tile[e] = Elem<T>::load(in + (size_t)nb * a.in_step + o);
+      }
+    }
+    __syncthreads();
+    if (active) {
+      const int j = lt / BI, i = lt - (lt / BI) * BI;
+      T *ob = out + (size_t)nbr[13] * a.out_step;
+#pragma unroll 1
+      for (int k = 0; k < BK; ++k) {
+        const AT *c = tile + ((k + R) * EJ + (j + R)) * EI + (i + R);
+        const AT v = stencil_point<AT, EJ, EI, R, FAM, ACC>(c, tp);
+        const int o = RM ? (k * BJ + j) * BI + i : a.L.offset(k, j, i);
+        Elem<T>::store(ob + o, v);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int BK, int BJ, int BI, int R, int FAM, bool RM, int ACC>
+int launch_sweep(const SweepArgs &a, const Taps &tp, cudaStream_t s) {
+  typedef typename Elem<T>::acc AT;
+  constexpr int TPB = BJ * BI;
+  constexpr int NT = sweep_threads(TPB);
+  constexpr int NB = NT / TPB;
+  constexpr int TILE = (BK + 2 * R) * (BJ + 2 * R) * (BI + 2 * R);
+  constexpr size_t smem = sizeof(AT) * TILE * NB + sizeof(unsigned) * 28 * NB;
+  static_assert(smem <= 227 * 1024, "tile too large");
+  auto kern = sweep_kernel<T, BK, BJ, BI, R, FAM, RM, ACC>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(sweep)");
+  }
+  long long grid = ((long long)a.nlist + NB - 1) / NB;
+  if (grid > (1ll << 30)) grid = 1ll << 30;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, NT, smem, s>>>(a, tp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "sweep kernel launch");
+  return BK_OK;
+}
+
+// Which instantiation a sweep needs.
+struct SweepPlan {
+  int dtype;
+  int shape;  // 0: 8x8x8, 1: 4x4x4, 2: 16x8x8, 3: 8x8x32
+  bool rm;
+  int fam;
+  int r;
+  int acc;
+};
+
+int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s);
+int sweep_dispatch_f32(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s);
+int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s);
+
+}  // namespace bk

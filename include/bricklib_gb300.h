@@ -1,0 +1,189 @@
+/*
+ * bricklib_gb300.h -- C ABI of the GB300 brick stencil engine (libbrick_gb300.so).
+ *
+ * This is the boundary a bricklib user binds instead of the reference's device
+ * layer.  Every entry point is plain C: device pointers, host pointers, sizes and
+ * a cudaStream_t passed as `void *` (NULL = the legacy default stream).  No call
+ * exits, traps or throws; each returns a bk_status and leaves a message for
+ * bk_last_error() (thread-local).  Calls are stream-ordered and do not
+ * synchronise unless their description says so.
+ *
+ * Data model (the reference's, include/brick.h):
+ *   BrickStorage  `chunks` chunks of `step` elements each (brick.h:53-82)
+ *   BrickInfo<3>  unsigned adj[nbricks][27]; slot (dk+1)*9+(dj+1)*3+(di+1) holds the
+ *                 storage index of the neighbour at (dk,dj,di), 13 = the brick itself
+ *                 (brick.h:96-127)
+ *   Brick         a field inside the storage: element (k,j,i) of brick b lives at
+ *                 dat[adj-resolved b * step + offset + layout(k,j,i)] (brick.h:353-395)
+ * layout(k,j,i) is the vector-fold order of _BrickAccessor (brick.h:213-327): with
+ * brick dims (BK,BJ,BI) and fold (FK,FJ,FI) the vector index is
+ * ((k/FK)*(BJ/FJ) + j/FJ)*(BI/FI) + i/FI and the lane ((k%FK)*FJ + j%FJ)*FI + i%FI.
+ * Triples are always (k, j, i) with i contiguous.
+ */
+#ifndef BRICKLIB_GB300_H
+#define BRICKLIB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BK_ABI_VERSION 1
+#define BK_MAX_TAPS 343 /* a radius-3 cube */
+
+typedef enum bk_status {
+  BK_OK = 0,
+  BK_ERR_ARG = 1,         /* invalid argument (message says which) */
+  BK_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  BK_ERR_NOMEM = 3,       /* device or host allocation failed */
+  BK_ERR_UNSUPPORTED = 4, /* valid request this build has no kernel for */
+  BK_ERR_BOUNDS = 5,      /* a kernel met an out-of-range brick index and skipped it */
+  BK_ERR_BUDGET = 6,      /* serving: request exceeds the HBM budget */
+  BK_ERR_STATE = 7,       /* call not valid in the object's current state */
+  BK_ERR_TIMEOUT = 8      /* a bounded device wait gave up */
+} bk_status;
+
+typedef enum bk_dtype { BK_F64 = 0, BK_F32 = 1, BK_BF16 = 2 } bk_dtype;
+
+/* Arithmetic of a sweep.
+ * BK_ACC_NATIVE      accumulate in the storage type (FP32 for BF16 storage)
+ * BK_ACC_COMPENSATED FP32/BF16 storage: FP32 accumulation with Neumaier compensation
+ * BK_ACC_FLOATFLOAT  FP64 storage: products and sums in float-float (pairs of FP32,
+ *                    error-free transforms of Dekker 1971 / Knuth TwoSum), relative
+ *                    error below 1e-13 per point; the FP64 units are not used */
+typedef enum bk_acc { BK_ACC_NATIVE = 0, BK_ACC_COMPENSATED = 1, BK_ACC_FLOATFLOAT = 2 } bk_acc;
+
+/* Brick dims and vector fold, (k, j, i); a fold of 1 means that axis is not folded.
+ * Brick<Dim<8,8,8>, Dim<4,8>> is {{8,8,8},{1,4,8}}. */
+typedef struct bk_layout {
+  int bdim[3];
+  int fold[3];
+} bk_layout;
+
+/* One field of a BrickStorage on the device: Brick(bInfo, storage, offset). */
+typedef struct bk_field {
+  void *dat;     /* device pointer to BrickStorage::dat */
+  long chunks;   /* BrickStorage::chunks */
+  size_t step;   /* BrickStorage::step, elements per chunk */
+  size_t offset; /* Brick offset within a chunk, elements */
+  int dtype;     /* bk_dtype of the elements */
+} bk_field;
+
+/* A stencil: out(k,j,i) = sum_t coeff[t] * in(k+off[t][0], j+off[t][1], i+off[t][2]).
+ * The reference compiles each stencil from a Python script (stencils/7pt.py, mpi*.py)
+ * into one kernel; here the tap list is data. |offset| on each axis must not exceed
+ * the brick dim on that axis (the accessor reaches one neighbour brick, brick.h:232-245). */
+typedef struct bk_stencil {
+  int npoints;
+  int offsets[BK_MAX_TAPS][3];
+  double coeff[BK_MAX_TAPS];
+} bk_stencil;
+
+/* ------------------------------------------------------------------ runtime */
+
+int bk_abi_version(void);
+/* Message of the last failed call on this host thread ("" if none). */
+const char *bk_last_error(void);
+/* Select the CUDA device for this host thread. */
+int bk_set_device(int device);
+int bk_device_synchronize(void);
+int bk_stream_synchronize(void *stream);
+
+/* Device memory.  bk_device_malloc replaces gpuMalloc in movBrickInfo /
+ * movBrickStorage (include/brick-gpu.h:42-103); bk_device_free replaces the
+ * gpuFree deleter of the device BrickStorage (brick-gpu.h:97-101). */
+int bk_device_malloc(void **dptr, size_t bytes);
+int bk_device_free(void *dptr);
+/* Page-locked host memory for copies that overlap with kernels. */
+int bk_host_malloc(void **hptr, size_t bytes);
+int bk_host_free(void *hptr);
+/* Stream-ordered copy; kind: 0 host->device, 1 device->host, 2 device->device. */
+int bk_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream);
+int bk_memset(void *dptr, int value, size_t bytes, void *stream);
+
+/* movBrickInfo(bInfo, cudaMemcpyHostToDevice) (include/brick-gpu.h:42-55):
+ * allocates nbricks*27 unsigned on the device and copies the adjacency list.
+ * Synchronous, like the reference's cudaMemcpy. Free with bk_device_free. */
+int bk_info_to_device(const unsigned *adj_host, unsigned nbricks, unsigned **adj_dev);
+/* movBrickStorage(bStorage, cudaMemcpyHostToDevice) (include/brick-gpu.h:84-103):
+ * allocates chunks*step elements and copies them.  Synchronous. */
+int bk_storage_to_device(const void *host, long chunks, size_t step, int dtype, void **dev);
+/* movBrickStorage(bStorage, cudaMemcpyDeviceToHost) into caller memory.  Synchronous. */
+int bk_storage_to_host(const void *dev, long chunks, size_t step, int dtype, void *host);
+
+/* Measured FMA rate of the current device for BK_F64 or BK_F32 (flop/s, an FMA counted
+ * as 2), from a kernel of independent FMA chains timed with CUDA events on `stream`.
+ * Synchronous.  Used as the compute roofline of the sweep; no reference counterpart. */
+int bk_measure_fma_rate(int dtype, void *stream, double *flops_per_s);
+
+/* Seeded synthetic input on the device: element p of dat (n elements of dtype) becomes
+ * lo + (hi - lo) * u with u = (splitmix64(seed + p) >> 11) * 2^-53, in separately
+ * rounded double arithmetic, then converted to the storage type.  Stands in for the
+ * reference's unseeded randomArray (src/multiarray.cpp:13-40). */
+int bk_fill_uniform(void *dat, size_t n, int dtype, uint64_t seed, double lo, double hi, void *stream);
+
+/* ------------------------------------------------------------------ the sweep */
+
+/* Validate a stencil for a layout; on success writes the radius (max |offset|) and the
+ * kernel family used: 1 star (taps on the axes), 2 cube (full (2r+1)^3 box), 0 generic. */
+int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, int *family);
+
+/* One stencil sweep over a brick list.  Replaces the per-brick CUDA kernels of the
+ * reference -- d3pt7_brick / d3pt7_brick_trans (stencils/3axis.cu:12-37), brick_kernel
+ * (weak/main.cu:35-43, strong/main.cu:85-111) -- and their launch (one kernel over the
+ * listed bricks instead of one 32-thread block per grid position, weak/main.cu:277-282).
+ *   adj        device BrickInfo adjacency, nbricks x 27
+ *   in, out    fields (may share a storage, e.g. interleaved bIn/bOut at offsets 0 and 512,
+ *              stencils/3axis.cu:119-121; in and out must not overlap element-wise)
+ *   blist      device list of nlist brick indices to compute (e.g. the interior bricks
+ *              grid[GB..STRIDEB-GB)^3 of 3axis.cu:167)
+ * Neighbour or list indices >= chunks/nbricks are clamped to brick 0 and reported by
+ * bk_error_flags() as BK_ERR_BOUNDS; the kernel never reads outside the storage. */
+int bk_sweep(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
+             const unsigned *blist, unsigned nlist, const bk_stencil *st, const bk_layout *lay,
+             int acc, void *stream);
+
+/* Reads and clears the device error word set by kernels of this library on the
+ * current device (synchronises the stream).  *flags = 0 when all launches were clean;
+ * bit 0: out-of-range brick index clamped; bit 1: bounded wait timed out. */
+int bk_error_flags(void *stream, int *flags);
+
+/* ------------------------------------------------------------------ ghost zones */
+
+/* Ghost-zone fill / periodic wrap on the device.  For every (dst, src) pair of brick
+ * storage indices copies the field's BRICKSIZE elements of brick src into brick dst.
+ * Replaces, on one GPU, the periodic BrickDecomp::exchange of a single rank
+ * (include/brick-mpi.h:466-499 on the periodic communicator of weak/args.cpp:105-108)
+ * and the D2H / MPI / H2D round trip around it (weak/main.cu:251-275). */
+int bk_ghost_fill(const unsigned *pairs, unsigned npairs, const bk_field *f, const bk_layout *lay,
+                  void *stream);
+
+/* Host helper: periodic (dst, src) plan for an init_grid layout of nb+2*gb bricks per axis
+ * (gb ghost bricks each side, grid as returned by init_grid).  Writes up to `cap` pairs
+ * and returns the count needed in *npairs (call with pairs = NULL to size). */
+int bk_periodic_plan(const unsigned *grid, const long nb[3], const long gb[3], unsigned *pairs,
+                     long cap, long *npairs);
+
+/* Batched contiguous copies inside device memory, one block per link:
+ * the reference's RegionLink / cudaCopy (strong/main.cu:60-83).  links: device array of
+ * nlinks {from, to, bytes} triples (uint64 each); bytes must be a multiple of 8. */
+int bk_region_copy(const uint64_t *links, unsigned nlinks, void *stream);
+
+/* ------------------------------------------------------------------ time steps */
+
+/* T time steps, ping-pong between fields a and b (weak/main.cu:277-282): before every
+ * `fill_every`-th step (0 = never) the ghost plan is applied to the current input field,
+ * then the sweep runs over blist.  After the call the newest values are in a when T is
+ * even and in b when T is odd.  With use_graph != 0 the T steps are captured once into a
+ * CUDA graph and replayed (launch-bound small domains). */
+int bk_steps(const unsigned *adj, unsigned nbricks, const bk_field *a, const bk_field *b,
+             const unsigned *blist, unsigned nlist, const unsigned *pairs, unsigned npairs,
+             const bk_stencil *st, const bk_layout *lay, int acc, int steps, int fill_every,
+             int use_graph, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BRICKLIB_GB300_H */

@@ -1,0 +1,220 @@
+"""Parity of the CUDA sweep, ghost fill and time stepping with the oracle and the
+golden vectors of bricklib's own CPU brick path.  All calls go through the C ABI.
+
+Tolerances: FP64 uses compareBrick's mixed test (brickcompare.h:37) with tol 1e-12;
+FP32 / BF16 storage are held to a normwise bound max|d| / max|ref| against the FP64
+oracle (1e-5 for FP32, 2^-7 for BF16, whose inputs and outputs are rounded to 8 bits).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from bricklib_gb300 import _abi, bricks as B, stencils
+from bricklib_gb300._abi import BK_ACC_COMPENSATED, BK_ACC_NATIVE, BK_BF16, BK_F32, BK_F64
+from bricklib_gb300.domain import GridDomain
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-12
+
+
+def mixed_ok(a, b, tol=TOL64):
+    d = np.abs(a - b)
+    return bool(np.all((d < tol) | (d < (np.abs(a) + np.abs(b)) * tol))), float(d.max(initial=0))
+
+
+def normwise(a, ref):
+    return float(np.abs(a - ref).max() / max(np.abs(ref).max(), 1e-300))
+
+
+def device_sweep(n, st, dtype=BK_F64, layout=B.DEFAULT_LAYOUT, acc=BK_ACC_NATIVE, seed=1234, arr=None):
+    dom = GridDomain(n, layout=layout, dtype=dtype)
+    if arr is None:
+        arr = stencils.uniform(seed, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, st, acc)
+    B.synchronize()
+    assert B.error_flags() == 0
+    dom.download()
+    return dom, arr, dom.interior_view(dom.get_field(1))
+
+
+def oracle_array(dom, arr, st):
+    out = np.zeros_like(arr, dtype=np.float64)
+    o, n = dom.org, dom.n
+    oracle.array_sweep(np.ascontiguousarray(arr, dtype=np.float64), out, o,
+                       (o[0] + n[0], o[1] + n[1], o[2] + n[2]), st.offsets(), st.coeff)
+    return dom.interior_view(out)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "sweep_*.npz"))),
+                         ids=lambda p: os.path.basename(p)[6:-4])
+def test_fp64_matches_reference_golden(path):
+    z = np.load(path)
+    st = stencils.custom("golden", [tuple(t) for t in z["offsets"]], z["coeff"])
+    lay = B.Layout((8, 8, 8), (1, 4, 8)) if int(z["layout"]) == 0 else B.Layout((4, 4, 4), (1, 4, 4))
+    _, _, got = device_sweep(int(z["n"]), st, layout=lay, seed=int(z["seed_in"]))
+    ok, md = mixed_ok(got, z["out"])
+    assert ok, f"max |diff| {md}"
+
+
+@pytest.mark.parametrize("name", stencils.PLAIN_SHAPES + ("heat7", "lap7"))
+def test_fp64_matches_oracle_64(name):
+    st = stencils.make(name, 7)
+    dom, arr, got = device_sweep(64, st, seed=42)
+    ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+    assert ok, f"{name}: max |diff| {md}"
+
+
+LAYOUTS = [((8, 8, 8), (1, 1, 8)), ((8, 8, 8), (1, 2, 2)), ((8, 8, 8), (2, 4, 4)), ((4, 4, 4), (1, 4, 4)),
+           ((16, 8, 8), (1, 4, 8)), ((8, 8, 32), (1, 1, 32)), ((8, 8, 32), (1, 4, 8))]
+
+
+@pytest.mark.parametrize("bdim,fold", LAYOUTS, ids=lambda x: "x".join(map(str, x)))
+@pytest.mark.parametrize("name", ["star7", "star13", "cube27", "cube125"])
+def test_fp64_layouts(bdim, fold, name):
+    st = stencils.make(name, 3)
+    if st.radius > min(bdim):
+        pytest.skip("radius beyond the brick")
+    n = (32, 32, 64) if bdim[2] == 32 else (32, 32, 32)
+    dom, arr, got = device_sweep(n, st, layout=B.Layout(bdim, fold), seed=9,
+                                 arr=None)
+    ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+    assert ok, f"max |diff| {md}"
+
+
+def test_generic_family_19pt():
+    taps = [t for t in stencils.cube_taps(1)[0] if sum(1 for a in t if a) <= 2]
+    st = stencils.custom("d3pt19", taps, stencils.uniform(5, len(taps), 0, 1))
+    assert B.stencil_family(st)[1] == 0
+    dom, arr, got = device_sweep(32, st, seed=3)
+    ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+    assert ok, f"max |diff| {md}"
+
+
+@pytest.mark.parametrize("name", stencils.PLAIN_SHAPES)
+@pytest.mark.parametrize("acc", [BK_ACC_NATIVE, BK_ACC_COMPENSATED])
+def test_fp32_against_fp64_oracle(name, acc):
+    st = stencils.make(name, 11)
+    dom, arr, got = device_sweep(64, st, dtype=BK_F32, acc=acc, seed=5)
+    ref = oracle_array(dom, arr.astype(np.float32).astype(np.float64), st)
+    assert normwise(got, ref) <= 1e-5
+
+
+def test_compensated_beats_native_on_cube125():
+    st = stencils.make("cube125", 2)
+    dom, arr, nat = device_sweep(64, st, dtype=BK_F32, acc=BK_ACC_NATIVE, seed=8)
+    _, _, comp = device_sweep(64, st, dtype=BK_F32, acc=BK_ACC_COMPENSATED, arr=arr)
+    ref = oracle_array(dom, arr.astype(np.float32).astype(np.float64), st)
+    # the FP32 output rounding (2^-24 relative) bounds both; compensation removes most of the rest
+    assert np.sqrt(np.mean((comp - ref) ** 2)) <= np.sqrt(np.mean((nat - ref) ** 2)) * 1.01
+
+
+@pytest.mark.parametrize("name", ["star7", "cube125"])
+def test_bf16_against_fp64_oracle(name):
+    st = stencils.make(name, 4)
+    dom, arr, got = device_sweep(32, st, dtype=BK_BF16, acc=BK_ACC_COMPENSATED, seed=6)
+    arr_b = B.bf16_to_f32(B.f32_to_bf16(arr.astype(np.float32))).astype(np.float64)
+    ref = oracle_array(dom, arr_b, st)
+    assert normwise(got, ref) <= 2.0 ** -7
+
+
+def test_interleaved_equals_separate_storages():
+    st = stencils.make("star13", 1)
+    dom, arr, inter = device_sweep(32, st, seed=2)
+    # separate storages: in and out each in their own BrickStorage
+    d1 = GridDomain(32, nfields=1)
+    d1.set_field(0, arr)
+    d1.upload()
+    out_st = B.BrickStorage.allocate_device(d1.nbricks, d1.step)
+    B.brickSweep(d1.brick(0), B.Brick(d1.dev_info, out_st, 0), d1.dev_interior, st)
+    host = B.movBrickStorage(out_st, to_device=False)
+    d1.storage.host[:] = host.host
+    np.testing.assert_array_equal(d1.interior_view(d1.get_field(0)), inter)
+
+
+def test_ghost_fill_matches_oracle_plan():
+    dom = GridDomain(32)
+    arr = stencils.uniform(17, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    plan = dom.periodic_plan()
+    B.ghostFill(plan, dom.brick(0))
+    B.synchronize()
+    dom.download()
+    want = oracle.Domain(32)
+    dat = want.alloc()
+    want.to_bricks(arr, dat, 0)
+    oracle.apply_plan(dat, want.step, 0, want.bsize, plan.host)
+    np.testing.assert_array_equal(dom.storage.host, dat)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_time_steps_with_periodic_fill(use_graph):
+    n, steps = 32, 10
+    st = stencils.make("heat7")
+    dom = GridDomain(n)
+    o = dom.org[0]
+    arr = oracle.fill_sines(dom.adims, (o,) * 3, (n,) * 3, 8, 123, 1e-3)
+    dom.set_field(0, arr)
+    dom.upload()
+    newest = B.timeSteps(dom.brick(0), dom.brick(1), dom.dev_interior, st, steps, plan=dom.periodic_plan(),
+                         fill_every=1, use_graph=use_graph)
+    B.synchronize()
+    dom.download()
+    assert newest.offset == (0 if steps % 2 == 0 else dom.bsize)
+    got = dom.interior_view(dom.get_field(0 if steps % 2 == 0 else 1))
+    a, b = arr.copy(), np.zeros_like(arr)
+    for _ in range(steps):
+        oracle.array_periodic_fill(a, (o,) * 3, (n,) * 3, (8, 8, 8))
+        oracle.array_sweep(a, b, (o,) * 3, (o + n,) * 3, st.offsets(), st.coeff)
+        a, b = b, a
+    ok, md = mixed_ok(got, dom.interior_view(a))
+    assert ok, f"max |diff| {md}"
+
+
+def test_graph_and_plain_steps_bitwise_equal():
+    res = []
+    for g in (False, True):
+        dom = GridDomain(32, dtype=BK_F32)
+        arr = stencils.uniform(77, int(np.prod(dom.adims))).reshape(dom.adims)
+        dom.set_field(0, arr)
+        dom.upload()
+        B.timeSteps(dom.brick(0), dom.brick(1), dom.dev_interior, stencils.make("cube27", 1), 7,
+                    plan=dom.periodic_plan(), use_graph=g)
+        B.synchronize()
+        dom.download()
+        res.append(dom.storage.host.copy())
+    np.testing.assert_array_equal(res[0], res[1])
+
+
+def test_out_of_range_adjacency_is_clamped_and_flagged():
+    dom = GridDomain(16, device=False)
+    bad = dom.bInfo.adj.copy()
+    victim = dom.interior[0]
+    bad[victim, 14] = dom.nbricks + 1000  # neighbour (0,0,+1) points past the storage
+    dom.bInfo = B.BrickInfo(dom.nbricks, bad)
+    arr = stencils.uniform(1, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.to_device()
+    B.error_flags()  # clear
+    B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, stencils.make("star7", 1))
+    B.synchronize()
+    assert B.error_flags() & 1
+    # a list entry past nbricks is skipped and flagged as well
+    lst = B.BrickList(np.array([dom.nbricks + 5, dom.interior[1]], dtype=np.uint32))
+    B.brickSweep(dom.brick(0), dom.brick(1), lst, stencils.make("star7", 1))
+    B.synchronize()
+    assert B.error_flags() & 1
+    assert B.error_flags() == 0  # reading clears
+
+
+def test_empty_brick_list_is_a_no_op():
+    dom = GridDomain(16)
+    B.brickSweep(dom.brick(0), dom.brick(1), B.BrickList(np.zeros(0, np.uint32)), stencils.make("star7", 1))
+    B.synchronize()

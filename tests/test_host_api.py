@@ -1,0 +1,96 @@
+"""CPU tests of the host side: the C ABI library loads and exports what the header
+declares, host-only ABI calls behave, and the reference-named host API matches
+the oracle."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from bricklib_gb300 import _abi, bricks as B, stencils
+from bricklib_gb300.domain import GridDomain
+from oracle import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(bk_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _abi.lib()
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    # every declared symbol has a ctypes signature in the binding
+    assert not [n for n in names if n not in _abi.SIGNATURES], "binding lags the header"
+    assert L.bk_abi_version() == 1
+
+
+def test_stencil_families():
+    lay = B.Layout()
+    for name, fam in [("star7", 1), ("star13", 1), ("star25", 1), ("cube27", 2), ("cube125", 2), ("heat7", 1)]:
+        r, f = B.stencil_family(stencils.make(name, 1), lay)
+        assert f == fam, name
+        assert r == stencils.make(name, 1).radius
+    # a 19-point stencil has no dedicated family: generic
+    taps = [t for t in stencils.cube_taps(1)[0] if sum(1 for a in t if a) <= 2]
+    r, f = B.stencil_family(stencils.custom("d3pt19", taps, np.ones(len(taps))), lay)
+    assert (r, f) == (1, 0)
+    # a non-row-major fold routes everything to the generic family
+    r, f = B.stencil_family(stencils.make("star7", 1), B.Layout((8, 8, 8), (1, 2, 2)))
+    assert f == 0
+
+
+def test_stencil_errors_are_reported_not_raised_in_c():
+    bad = stencils.custom("far", [(0, 0, 9)], [1.0])
+    with pytest.raises(_abi.BkError) as e:
+        B.stencil_family(bad, B.Layout())
+    assert e.value.status == _abi.BK_ERR_ARG and "brick dim" in str(e.value)
+    with pytest.raises(_abi.BkError) as e:
+        B.stencil_family(stencils.custom("r5", [(0, 0, 5)], [1.0]), B.Layout((8, 8, 32), (1, 1, 32)))
+    assert e.value.status == _abi.BK_ERR_UNSUPPORTED
+
+
+def test_periodic_plan_abi_matches_oracle():
+    dom = GridDomain(16, device=False)
+    plan = B.GhostPlan.__new__(B.GhostPlan)
+    nb_c, gb_c = (C.c_long * 3)(*dom.nb), (C.c_long * 3)(*dom.gb)
+    cnt = C.c_long()
+    _abi.call("bk_periodic_plan", dom.grid.ctypes.data_as(C.c_void_p), nb_c, gb_c, None, 0, C.byref(cnt))
+    pairs = np.empty((cnt.value, 2), dtype=np.uint32)
+    _abi.call("bk_periodic_plan", dom.grid.ctypes.data_as(C.c_void_p), nb_c, gb_c,
+              pairs.ctypes.data_as(C.c_void_p), cnt.value, C.byref(cnt))
+    np.testing.assert_array_equal(pairs, oracle.periodic_plan(dom.grid, dom.nb, dom.gb))
+
+
+@pytest.mark.parametrize("bdim,fold", [((8, 8, 8), (1, 4, 8)), ((8, 8, 8), (2, 4, 4)), ((4, 4, 4), (1, 4, 4))])
+def test_copy_to_from_brick_matches_oracle(bdim, fold):
+    lay = B.Layout(bdim, fold)
+    dom = GridDomain(16, layout=lay, device=False)
+    arr = stencils.uniform(3, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    odom = oracle.Domain(16, bdim=bdim, fold=fold)
+    dat = odom.alloc()
+    odom.to_bricks(arr, dat, 0)
+    np.testing.assert_array_equal(dom.storage.host, dat)
+    np.testing.assert_array_equal(dom.get_field(0), odom.from_bricks(dat, 0))
+
+
+def test_bf16_rounding():
+    x = np.array([1.0, 1.00390625, 1.01171875, -3.5, 1e-3], dtype=np.float32)
+    back = B.bf16_to_f32(B.f32_to_bf16(x))
+    assert back[0] == 1.0 and back[1] == 1.0  # ties to even
+    assert back[2] == np.float32(1.015625)
+    assert back[3] == -3.5
+    assert abs(back[4] - 1e-3) / 1e-3 < 2 ** -8
