@@ -69,5 +69,24 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
+def build_cpp_driver(verbose: bool = False) -> str:
+    """The C++ drop-in driver of tests/cpp/single_gb300.cpp, linked against the library."""
+    src = os.path.join(ROOT, "tests", "cpp", "single_gb300.cpp")
+    exe = os.path.join(LIBDIR, "single_gb300")
+    deps = [src, LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
+        return exe
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+    cmd = ["g++", "-O2", "-fopenmp", "-std=c++17", "-I", INCLUDE, "-I", cuda_inc, src, "-o", exe,
+           "-L", LIBDIR, "-lbrick_gb300", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed on {src}:\n{r.stdout}\n{r.stderr}")
+    return exe
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
+    print(build_cpp_driver(verbose="-v" in sys.argv))

@@ -167,23 +167,24 @@ sweep_kernel(const SweepArgs a, const Taps tp) {
 
   for (long long base = (long long)blockIdx.x * NB; base < a.nlist; base += (long long)gridDim.x * NB) {
     const long long n = base + slot;
-    if (lt < 27) {
+    // all 27 slots are written every iteration, whatever the threads per brick (16 for 4^3)
+    for (int sl = lt; sl < 27; sl += TPB) {
       unsigned v = 0;
       int ok = 0;
       if (n < a.nlist) {
         const unsigned b = a.blist[n];
         if (b < a.nbricks) {
-          v = a.adj[(size_t)b * 27 + lt];
+          v = a.adj[(size_t)b * 27 + sl];
           ok = 1;
           // the centre entry is also the output brick: out of range skips the brick
-          if (lt == 13 && ((long long)v >= a.out_chunks || (long long)v >= a.in_chunks)) ok = 0;
+          if (sl == 13 && ((long long)v >= a.out_chunks || (long long)v >= a.in_chunks)) ok = 0;
           if ((long long)v >= a.in_chunks || !ok) { atomicOr(a.err, FLAG_BOUNDS); v = 0; }
-        } else if (lt == 13) {
+        } else if (sl == 13) {
           atomicOr(a.err, FLAG_BOUNDS);
         }
       }
-      nbr[lt] = v;
-      if (lt == 13) nbr[27] = ok;
+      nbr[sl] = v;
+      if (sl == 13) nbr[27] = ok;
     }
     __syncthreads();
     const bool active = nbr[27] != 0;

@@ -1,0 +1,120 @@
+// The reference's single-node CUDA test (single/cuda.cpp -> stencils/3axis.cu d3pt7cu)
+// written against the GB300 engine's source-compatible headers: the same init_grid /
+// BrickStorage / Brick / copyToBrick / movBrickInfo / movBrickStorage / compareBrick calls,
+// with the per-brick CUDA kernel replaced by brickSweep.  Runs the 7-point stencil of
+// 3axis.cu (coeff[0..6]) and the 13/25-point stars, 27- and 125-point cubes on an N^3
+// interior, and compares every result with the array kernel at 1e-12.
+// Exit status 0 and "result match" on success.
+#define BRICK_TOLERANCE 1e-12
+
+#include <cstdio>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#include "brick.h"
+#include "brick-gb300.h"
+#include "brickcompare.h"
+#include "bricksetup.h"
+
+#define N 64
+#define TILE 8
+#define GZ TILE
+#define PADDING 8
+#define STRIDE (N + 2 * (GZ + PADDING))
+#define STRIDEG (N + 2 * GZ)
+#define STRIDEB ((N + 2 * GZ) / TILE)
+#define GB (GZ / TILE)
+
+typedef Brick<Dim<8, 8, 8>, Dim<4, 8>> Brick3D;
+
+struct Tap { int dk, dj, di; };
+
+static std::vector<Tap> star(int r) {
+  std::vector<Tap> t{{0, 0, 0}};
+  for (int d = 1; d <= r; ++d) {
+    t.push_back({0, 0, d}); t.push_back({0, 0, -d});
+    t.push_back({0, d, 0}); t.push_back({0, -d, 0});
+    t.push_back({d, 0, 0}); t.push_back({-d, 0, 0});
+  }
+  return t;
+}
+
+static std::vector<Tap> cube(int r) {
+  std::vector<Tap> t;
+  for (int k = -r; k <= r; ++k)
+    for (int j = -r; j <= r; ++j)
+      for (int i = -r; i <= r; ++i) t.push_back({k, j, i});
+  return t;
+}
+
+int main() {
+  std::mt19937_64 mt(20261203);
+  std::uniform_real_distribution<bElem> u(-1, 1);
+
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<3>(grid_ptr, {STRIDEB, STRIDEB, STRIDEB});
+  auto grid = (unsigned(*)[STRIDEB][STRIDEB])grid_ptr;
+
+  // interior brick list on the device (the blocks of d3pt7_brick_trans, 3axis.cu:167)
+  std::vector<unsigned> interior;
+  for (long tk = GB; tk < STRIDEB - GB; ++tk)
+    for (long tj = GB; tj < STRIDEB - GB; ++tj)
+      for (long ti = GB; ti < STRIDEB - GB; ++ti) interior.push_back(grid[tk][tj][ti]);
+  unsigned *blist_dev = nullptr;
+  gpuCheck(bk_device_malloc((void **)&blist_dev, interior.size() * sizeof(unsigned)));
+  gpuCheck(bk_memcpy(blist_dev, interior.data(), interior.size() * sizeof(unsigned), 0, nullptr));
+
+  const long size = (long)STRIDE * STRIDE * STRIDE;
+  std::vector<bElem> in(size), out(size, 0.0);
+  for (auto &x : in) x = u(mt);
+  bElem(*arr_in)[STRIDE][STRIDE] = (bElem(*)[STRIDE][STRIDE])in.data();
+  bElem(*arr_out)[STRIDE][STRIDE] = (bElem(*)[STRIDE][STRIDE])out.data();
+
+  auto bSize = cal_size<8, 8, 8>::value;
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, bSize * 2);
+  Brick3D bIn(&bInfo, bStorage, 0);
+  Brick3D bOut(&bInfo, bStorage, bSize);
+  copyToBrick<3>({STRIDEG, STRIDEG, STRIDEG}, {PADDING, PADDING, PADDING}, {0, 0, 0}, in.data(), grid_ptr, bIn);
+
+  BrickInfo<3> bInfo_dev = movBrickInfo(bInfo, cudaMemcpyHostToDevice);
+  BrickStorage bStorage_dev = movBrickStorage(bStorage, cudaMemcpyHostToDevice);
+  Brick3D bIn_dev(&bInfo_dev, bStorage_dev, 0);
+  Brick3D bOut_dev(&bInfo_dev, bStorage_dev, bSize);
+
+  struct Case { const char *name; std::vector<Tap> taps; };
+  std::vector<Case> cases = {{"d3pt7", star(1)}, {"d3pt13", star(2)}, {"d3pt25", star(4)},
+                             {"d3pt27", cube(1)}, {"d3pt125", cube(2)}};
+  for (auto &c : cases) {
+    BrickStencil st;
+    std::vector<bElem> coeff;
+    for (auto &t : c.taps) {
+      coeff.push_back(u(mt));
+      st.add(t.dk, t.dj, t.di, coeff.back());
+    }
+    // array kernel (3axis.cpp:32-37 generalised to the tap list)
+    for (long k = PADDING + GZ; k < PADDING + GZ + N; ++k)
+      for (long j = PADDING + GZ; j < PADDING + GZ + N; ++j)
+        for (long i = PADDING + GZ; i < PADDING + GZ + N; ++i) {
+          bElem v = 0;
+          for (size_t t = 0; t < c.taps.size(); ++t)
+            v += coeff[t] * arr_in[k + c.taps[t].dk][j + c.taps[t].dj][i + c.taps[t].di];
+          arr_out[k][j][i] = v;
+        }
+    brickSweep(bIn_dev, bOut_dev, blist_dev, (unsigned)interior.size(), st);
+    int flags = 0;
+    gpuCheck(bk_error_flags(nullptr, &flags));
+    if (flags) throw std::runtime_error("device error flags");
+    BrickStorage back = movBrickStorage(bStorage_dev, cudaMemcpyDeviceToHost);
+    Brick3D bOut_host(&bInfo, back, bSize);
+    if (!compareBrick<3>({N, N, N}, {PADDING, PADDING, PADDING}, {GZ, GZ, GZ}, out.data(), grid_ptr, bOut_host))
+      throw std::runtime_error(std::string(c.name) + ": result mismatch!");
+    printf("%s match\n", c.name);
+  }
+  gpuCheck(bk_device_free(blist_dev));
+  gpuCheck(bk_device_free(bInfo_dev.adj));
+  free(grid_ptr);
+  free(bInfo.adj);
+  printf("result match\n");
+  return 0;
+}

@@ -94,3 +94,29 @@ def test_bf16_rounding():
     assert back[2] == np.float32(1.015625)
     assert back[3] == -3.5
     assert abs(back[4] - 1e-3) / 1e-3 < 2 ** -8
+
+
+def test_cpp_headers_match_reference_accessor(tmp_path):
+    """include/brick.h + bricksetup.h compiled with g++: accessor offsets and init_grid
+    equal the golden vectors made by the reference's own headers."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    exe, out = tmp_path / "host_api_check", tmp_path / "out.bin"
+    subprocess.check_call(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cpp", "host_api_check.cpp"), "-o", str(exe)])
+    subprocess.check_call([str(exe), str(out)])
+    raw = open(out, "rb").read()
+    z = np.load(os.path.join(ROOT, "tests", "golden", "layouts.npz"))
+    pos = 0
+    for lid in range(7):
+        want = z[f"offsets_{lid}"]
+        got = np.frombuffer(raw, dtype=np.int64, count=len(want), offset=pos)
+        pos += 8 * len(want)
+        np.testing.assert_array_equal(got, want, err_msg=f"layout {lid}")
+    g = np.load(os.path.join(ROOT, "tests", "golden", "init_grid.npz"))
+    grid = np.frombuffer(raw, dtype=np.uint32, count=60, offset=pos)
+    adj = np.frombuffer(raw, dtype=np.uint32, count=60 * 27, offset=pos + 240)
+    np.testing.assert_array_equal(grid, g["grid"])
+    np.testing.assert_array_equal(adj, g["adj"])
