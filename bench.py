@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--shapes", default=",".join(SHAPES))
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-alt", action="store_true")
     return p.parse_args()
 
 
@@ -228,6 +229,37 @@ def run_ours(args):
                             "peak": round(fp64_rate.value / 1e12, 3),
                             "peak_source": f"measured {'FP64' if dtype == _abi.BK_F64 else 'FP32'} FMA rate (bk_measure_fma_rate)"}}
 
+    # the other FP64 arithmetic mode on the same data: per-stencil rate and its normwise
+    # error against the first mode's output
+    alt = None
+    if dtype == _abi.BK_F64 and not args.no_alt:
+        alt_acc = _abi.BK_ACC_FLOATFLOAT if acc == _abi.BK_ACC_NATIVE else _abi.BK_ACC_NATIVE
+        alt = {"accumulation": "floatfloat" if alt_acc == _abi.BK_ACC_FLOATFLOAT else "native", "per_stencil": {}}
+        nb = nbricks * bsize
+        ref_out, alt_out = np.empty(nb), np.empty(nb)
+        for name in shapes:
+            sweep(name)
+            B.memcpy(ref_out.ctypes.data, s_out.ptr, ref_out.nbytes, 1, sp)
+            B.brickSweep(b_in, b_out, blist, csts[name], alt_acc, stream=sp)
+            torch.cuda.synchronize()
+            ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ea.record(stream)
+            for _ in range(K):
+                B.brickSweep(b_in, b_out, blist, csts[name], alt_acc, stream=sp)
+            eb.record(stream)
+            torch.cuda.synchronize()
+            ms = ea.elapsed_time(eb) / K
+            B.memcpy(alt_out.ctypes.data, s_out.ptr, alt_out.nbytes, 1, sp)
+            B.synchronize(sp)
+            live = np.concatenate([np.arange(int(b) * bsize, int(b) * bsize + bsize) for b in interior[:4096]])
+            err = float(np.abs(alt_out[live] - ref_out[live]).max() / np.abs(ref_out[live]).max())
+            gst = points / (ms * 1e-3) / 1e9
+            alt["per_stencil"][name] = {"ms": round(ms, 4), "gstencil_s": round(gst, 2),
+                                        "hbm_frac": round(gst * 1e9 * bytes_pt / (hbm * 1e9), 4),
+                                        "normwise_err_vs_main": err}
+        tot = sum(v["ms"] for v in alt["per_stencil"].values())
+        alt["value"] = round(len(shapes) * points / (tot * 1e-3) / 1e9, 3)
+
     # end to end through the public API: pinned host input -> device, sweeps, results -> host
     e2e = None
     if not args.no_e2e:
@@ -269,7 +301,7 @@ def run_ours(args):
                            "interior_points": points, "bricks": nbricks, "accumulation": args.acc,
                            "l2": f"no flush: inputs {nbricks * bsize * esize / 1e9:.2f} GB per field > 129 MB L2",
                            "parallelism": f"replicas x{ws}"},
-                "per_stencil": per_shape, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "per_stencil": per_shape, "alt_mode": alt, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": K * len(shapes), "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -83,6 +83,7 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
     else if (fam == FAM_CUBE) idx = ((dk + r) * (2 * r + 1) + (dj + r)) * (2 * r + 1) + (di + r);
     tp->c[idx] = st->coeff[t];
     tp->cf[idx] = (float)st->coeff[t];
+    tp->cl[idx] = (float)(st->coeff[t] - (double)tp->cf[idx]);
     tp->toff[idx] = (dk * EJ + dj) * EI + di;
   }
   return BK_OK;
@@ -109,6 +110,8 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
   if (acc == BK_ACC_NATIVE) plan->acc = ACCM_NATIVE;
   else if (acc == BK_ACC_COMPENSATED && in->dtype != BK_F64) plan->acc = ACCM_COMP;
   else if (acc == BK_ACC_COMPENSATED) return fail(BK_ERR_UNSUPPORTED, "compensated accumulation is for FP32 / BF16 storage");
+  else if (acc == BK_ACC_FLOATFLOAT && in->dtype == BK_F64) plan->acc = ACCM_FF;
+  else if (acc == BK_ACC_FLOATFLOAT) return fail(BK_ERR_UNSUPPORTED, "float-float arithmetic is for FP64 storage");
   else return fail(BK_ERR_UNSUPPORTED, "accumulation mode not available in this build");
   int *err = device_error_word();
   if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");

@@ -19,6 +19,7 @@ namespace bk {
 int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s) {
   if (p.shape == 0) {
     BK_SHAPE_SET(8, 8, 8, ACCM_NATIVE)
+    BK_SHAPE_SET(8, 8, 8, ACCM_FF)
 
   } else if (p.shape == 1) {
     BK_SHAPE_SET(4, 4, 4, ACCM_NATIVE)

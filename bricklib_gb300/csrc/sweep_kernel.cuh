@@ -20,7 +20,7 @@
 namespace bk {
 
 enum Family { FAM_GENERIC = 0, FAM_STAR = 1, FAM_CUBE = 2 };
-enum AccMode { ACCM_NATIVE = 0, ACCM_COMP = 1 };
+enum AccMode { ACCM_NATIVE = 0, ACCM_COMP = 1, ACCM_FF = 2 };
 
 struct SweepArgs {
   const unsigned *adj;
@@ -41,7 +41,8 @@ struct SweepArgs {
 struct Taps {
   int n;
   int toff[BK_MAX_TAPS];  // generic family: tap offset in tile elements from the centre
-  float cf[BK_MAX_TAPS];
+  float cf[BK_MAX_TAPS];   // coefficient rounded to float (the high part)
+  float cl[BK_MAX_TAPS];   // float(c - cf): the low part, for float-float arithmetic
   double c[BK_MAX_TAPS];
 };
 
@@ -61,6 +62,145 @@ __device__ __forceinline__ void neumaier(AT &s, AT &comp, AT p) {
   comp += (absval(s) >= absval(p)) ? ((s - t) + p) : ((p - t) + s);
   s = t;
 }
+
+// ---------------------------------------------------------------- float-float (FP64 storage)
+//
+// A double x is held as hi + lo, two floats obtained from its bit pattern with integer
+// operations only (the FP64 pipe of GB300 runs at 1/64 of the FP32 rate, and so do the
+// double<->float conversions): hi carries the sign, exponent and top 23 stored mantissa
+// bits (truncated), lo the next 23 bits, i.e. 47 significant bits, relative error
+// below 2^-47.  |x| must be below 2^128; |x| below 2^-126 reads as 0.
+__device__ __forceinline__ float2 split_f64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned sign = h32 & 0x80000000u;
+  const int e = (int)((h32 >> 20) & 0x7FFu) - 1023;
+  const unsigned m23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
+  float hi, lo;
+  if (e >= -126 && e <= 127) {
+    hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | m23);
+    // next 23 mantissa bits; bit 0 weighs 2^(e-46).  (2^23 + r) * 2^(e-46) - 2^23 * 2^(e-46)
+    // is r * 2^(e-46), exact
+    const unsigned r = (l32 & 0x1FFFFFFFu) >> 6;
+    const int el = e + 104;
+    lo = el >= 1 ? __uint_as_float(((unsigned)el << 23) | r) - __uint_as_float((unsigned)el << 23) : 0.0f;
+    lo = __uint_as_float(__float_as_uint(lo) | sign);
+  } else if (e > 127) {
+    hi = __uint_as_float(sign | 0x7F800000u);
+    lo = 0.0f;
+  } else {
+    hi = __uint_as_float(sign);
+    lo = 0.0f;
+  }
+  return make_float2(hi, lo);
+}
+
+// Knuth's TwoSum: s + err == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &err) {
+  s = a + b;
+  const float bp = s - a;
+  err = (a - (s - bp)) + (b - bp);
+}
+
+// The double nearest (within 2^-52 relative) to the float-float value h + l, |l| <= ulp(h)/2,
+// built from the two bit patterns with integer operations.
+__device__ __forceinline__ double ff_to_f64(float h, float l) {
+  const unsigned bh = __float_as_uint(h);
+  const unsigned eh = (bh >> 23) & 0xFFu;
+  if (eh == 0) return 0.0;
+  if (eh == 0xFFu) return __longlong_as_double((long long)(((unsigned long long)(bh & 0x80000000u) << 32) | 0x7FF0000000000000ull));
+  long long M = (long long)((1ull << 52) | ((unsigned long long)(bh & 0x7FFFFFu) << 29));
+  int E = (int)eh - 127 + 1023;
+  const unsigned bl = __float_as_uint(l);
+  const unsigned el = (bl >> 23) & 0xFFu;
+  if (el != 0) {
+    const long long ml = (long long)((1u << 23) | (bl & 0x7FFFFFu));
+    const int sh = (int)el - (int)eh + 29;  // <= 5
+    long long add = sh >= 0 ? (ml << sh) : (sh > -40 ? (ml >> (-sh)) : 0);
+    M += ((bl ^ bh) & 0x80000000u) ? -add : add;
+    if (M < (1ll << 52)) {
+      M <<= 1;
+      E -= 1;
+    }
+  }
+  const unsigned long long bits = ((unsigned long long)(bh & 0x80000000u) << 32) |
+                                  ((unsigned long long)E << 52) | ((unsigned long long)M & ((1ull << 52) - 1));
+  return __longlong_as_double((long long)bits);
+}
+
+// Dot2-style accumulation of c * x: (s, corr) with s + corr ~ sum of products.
+struct FFAcc {
+  float s, corr;
+  // products are formed with __fmul_rn so that they are never contracted into a
+  // following addition: TwoSum and the FMA error term need the rounded product itself
+  __device__ __forceinline__ void first(float ch, float cl, float2 x) {
+    s = __fmul_rn(ch, x.x);
+    corr = fmaf(ch, x.x, -s);
+    corr = fmaf(ch, x.y, corr);
+    corr = fmaf(cl, x.x, corr);
+  }
+  __device__ __forceinline__ void add(float ch, float cl, float2 x) {
+    const float p = __fmul_rn(ch, x.x);
+    float t, err;
+    two_sum(s, p, t, err);
+    s = t;
+    corr += fmaf(ch, x.x, -p) + err;
+    corr = fmaf(ch, x.y, corr);
+    corr = fmaf(cl, x.x, corr);
+  }
+  __device__ __forceinline__ double result() const {
+    float h, l;
+    two_sum(s, corr, h, l);
+    return ff_to_f64(h, l);
+  }
+};
+
+template <int EJ, int EI, int R, int FAM>
+__device__ __forceinline__ double stencil_point_ff(const float2 *__restrict__ c, const Taps &tp) {
+  constexpr int SJ = EI, SK = EJ * EI;
+  FFAcc a;
+  if (FAM == FAM_STAR) {
+    a.first(tp.cf[0], tp.cl[0], c[0]);
+#pragma unroll
+    for (int d = 1; d <= R; ++d) {
+      const int t = 1 + 6 * (d - 1);
+      a.add(tp.cf[t + 0], tp.cl[t + 0], c[d]);
+      a.add(tp.cf[t + 1], tp.cl[t + 1], c[-d]);
+      a.add(tp.cf[t + 2], tp.cl[t + 2], c[d * SJ]);
+      a.add(tp.cf[t + 3], tp.cl[t + 3], c[-d * SJ]);
+      a.add(tp.cf[t + 4], tp.cl[t + 4], c[d * SK]);
+      a.add(tp.cf[t + 5], tp.cl[t + 5], c[-d * SK]);
+    }
+  } else if (FAM == FAM_CUBE) {
+#pragma unroll
+    for (int dk = -R; dk <= R; ++dk)
+#pragma unroll
+      for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+        for (int di = -R; di <= R; ++di) {
+          const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+          const float2 x = c[dk * SK + dj * SJ + di];
+          if (t == 0) a.first(tp.cf[0], tp.cl[0], x);
+          else a.add(tp.cf[t], tp.cl[t], x);
+        }
+  } else {
+    a.first(tp.cf[0], tp.cl[0], c[tp.toff[0]]);
+    for (int t = 1; t < tp.n; ++t) a.add(tp.cf[t], tp.cl[t], c[tp.toff[t]]);
+  }
+  return a.result();
+}
+
+// Element type of the shared-memory tile and the load that fills it.
+template <typename T, int ACC>
+struct TileOf {
+  typedef typename Elem<T>::acc type;
+  static __device__ __forceinline__ type load(const T *p) { return Elem<T>::load(p); }
+};
+template <>
+struct TileOf<double, ACCM_FF> {
+  typedef float2 type;
+  static __device__ __forceinline__ float2 load(const double *p) { return split_f64(__ldg(p)); }
+};
 
 // One output point; c points at the centre element in the tile.
 template <typename AT, int EJ, int EI, int R, int FAM, int ACC>
@@ -148,7 +288,7 @@ __device__ __forceinline__ AT stencil_point(const AT *__restrict__ c, const Taps
 template <typename T, int BK, int BJ, int BI, int R, int FAM, bool RM, int ACC>
 __global__ void __launch_bounds__(sweep_threads(BJ * BI))
 sweep_kernel(const SweepArgs a, const Taps tp) {
-  typedef typename Elem<T>::acc AT;
+  typedef typename TileOf<T, ACC>::type AT;
   constexpr int TPB = BJ * BI;
   constexpr int NT = sweep_threads(TPB);
   constexpr int NB = NT / TPB;
@@ -199,7 +339,7 @@ sweep_kernel(const SweepArgs a, const Taps tp) {
         const int lk = kk - R - qk * BK, lj = jj - R - qj * BJ, li = ii - R - qi * BI;
         const unsigned nb = nbr[(qk + 1) * 9 + (qj + 1) * 3 + (qi + 1)];
         const int o = RM ? (lk * BJ + lj) * BI + li : a.L.offset(lk, lj, li);
-        tile[e] = Elem<T>::load(in + (size_t)nb * a.in_step + o);
+        tile[e] = TileOf<T, ACC>::load(in + (size_t)nb * a.in_step + o);
       }
     }
     __syncthreads();
@@ -209,7 +349,9 @@ sweep_kernel(const SweepArgs a, const Taps tp) {
 #pragma unroll 1
       for (int k = 0; k < BK; ++k) {
         const AT *c = tile + ((k + R) * EJ + (j + R)) * EI + (i + R);
-        const AT v = stencil_point<AT, EJ, EI, R, FAM, ACC>(c, tp);
+        typename Elem<T>::acc v;
+        if constexpr (ACC == ACCM_FF) v = stencil_point_ff<EJ, EI, R, FAM>(c, tp);
+        else v = stencil_point<AT, EJ, EI, R, FAM, ACC>(c, tp);
         const int o = RM ? (k * BJ + j) * BI + i : a.L.offset(k, j, i);
         Elem<T>::store(ob + o, v);
       }
@@ -220,7 +362,7 @@ sweep_kernel(const SweepArgs a, const Taps tp) {
 
 template <typename T, int BK, int BJ, int BI, int R, int FAM, bool RM, int ACC>
 int launch_sweep(const SweepArgs &a, const Taps &tp, cudaStream_t s) {
-  typedef typename Elem<T>::acc AT;
+  typedef typename TileOf<T, ACC>::type AT;
   constexpr int TPB = BJ * BI;
   constexpr int NT = sweep_threads(TPB);
   constexpr int NB = NT / TPB;
