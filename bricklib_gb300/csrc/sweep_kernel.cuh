@@ -148,6 +148,14 @@ struct FFAcc {
     corr = fmaf(ch, x.y, corr);
     corr = fmaf(cl, x.x, corr);
   }
+  // moves the correction into s (s + corr unchanged): keeps |corr| near ulp(s) so the
+  // FP32 rounding of later correction terms stays at the 2^-48 level
+  __device__ __forceinline__ void renorm() {
+    float t, e;
+    two_sum(s, corr, t, e);
+    s = t;
+    corr = e;
+  }
   __device__ __forceinline__ double result() const {
     float h, l;
     two_sum(s, corr, h, l);
@@ -170,6 +178,7 @@ __device__ __forceinline__ double stencil_point_ff(const float2 *__restrict__ c,
       a.add(tp.cf[t + 3], tp.cl[t + 3], c[-d * SJ]);
       a.add(tp.cf[t + 4], tp.cl[t + 4], c[d * SK]);
       a.add(tp.cf[t + 5], tp.cl[t + 5], c[-d * SK]);
+      a.renorm();
     }
   } else if (FAM == FAM_CUBE) {
 #pragma unroll
@@ -182,10 +191,14 @@ __device__ __forceinline__ double stencil_point_ff(const float2 *__restrict__ c,
           const float2 x = c[dk * SK + dj * SJ + di];
           if (t == 0) a.first(tp.cf[0], tp.cl[0], x);
           else a.add(tp.cf[t], tp.cl[t], x);
+          if (di == R) a.renorm();
         }
   } else {
     a.first(tp.cf[0], tp.cl[0], c[tp.toff[0]]);
-    for (int t = 1; t < tp.n; ++t) a.add(tp.cf[t], tp.cl[t], c[tp.toff[t]]);
+    for (int t = 1; t < tp.n; ++t) {
+      a.add(tp.cf[t], tp.cl[t], c[tp.toff[t]]);
+      if ((t & 7) == 7) a.renorm();
+    }
   }
   return a.result();
 }
