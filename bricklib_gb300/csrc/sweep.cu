@@ -75,6 +75,8 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   plan->shape = shape_of(L);
   if (!tp) return BK_OK;
   tp->n = n;
+  static thread_local int offs[BK_MAX_TAPS][3];
+  static thread_local int toff1[BK_MAX_TAPS];
   const int EJ = L.bj + 2 * GENERIC_R, EI = L.bi + 2 * GENERIC_R;
   for (int t = 0; t < n; ++t) {
     const int dk = st->offsets[t][0], dj = st->offsets[t][1], di = st->offsets[t][2];
@@ -84,8 +86,14 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
     tp->c[idx] = st->coeff[t];
     tp->cf[idx] = (float)st->coeff[t];
     tp->cl[idx] = (float)(st->coeff[t] - (double)tp->cf[idx]);
-    tp->toff[idx] = (dk * EJ + dj) * EI + di;
+    toff1[idx] = (dk * EJ + dj) * EI + di;
+    tp->toff[idx] = toff1[idx];
+    offs[idx][0] = dk;
+    offs[idx][1] = dj;
+    offs[idx][2] = di;
   }
+  plan->offs = offs;
+  plan->toff1 = toff1;
   return BK_OK;
 }
 
@@ -113,6 +121,15 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
   else if (acc == BK_ACC_FLOATFLOAT && in->dtype == BK_F64) plan->acc = ACCM_FF;
   else if (acc == BK_ACC_FLOATFLOAT) return fail(BK_ERR_UNSUPPORTED, "float-float arithmetic is for FP64 storage");
   else return fail(BK_ERR_UNSUPPORTED, "accumulation mode not available in this build");
+  // the pipelined kernel copies whole 16-byte (or brick-row) vectors: it needs a row-major
+  // layout and vector-aligned input addresses
+  {
+    const size_t es = dtype_size(in->dtype);
+    const size_t vb = (size_t)L.bi * es < 16 ? (size_t)L.bi * es : 16;
+    const size_t ve = vb / es;
+    plan->v2 = plan->rm && (reinterpret_cast<uintptr_t>(in->dat) % 16 == 0) && in->step % ve == 0 &&
+               in->offset % ve == 0 && !getenv("BK_SWEEP_ONESHOT");
+  }
   int *err = device_error_word();
   if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
   *a = SweepArgs{adj, nbricks, in->dat, in->step, in->offset, in->chunks,
@@ -120,7 +137,7 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
   return BK_OK;
 }
 
-static int dispatch(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s) {
+static int dispatch(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
   switch (p.dtype) {
     case BK_F64: return sweep_dispatch_f64(p, a, tp, s);
     case BK_F32: return sweep_dispatch_f32(p, a, tp, s);

@@ -1,0 +1,445 @@
+// Pipelined brick sweep for row-major brick layouts (sweep_kernel covers the rest).
+//
+// Persistent CTAs walk the brick list in groups of NB bricks.  For every group:
+//   * the 27 adjacency entries of each brick are staged in shared memory;
+//   * every thread issues its share of the group's gather as asynchronous global->shared
+//     copies (cp.async, 16 bytes where the layout allows) into one of two tile buffers,
+//     following a per-thread plan computed once at kernel start: each plan entry is one
+//     vector of the brick's neighbourhood -- centre brick, faces (stars) or the full
+//     (BK+2R) x (BJ+2R) x (BI+2RP) box (cubes) -- packed as (adjacency slot, source
+//     offset in the neighbour brick, destination offset in the tile);
+//   * while those copies are in flight the previous group is computed from the other
+//     buffer.
+// Compute: each thread owns one (j, i) column of a brick; the column's k-extended values
+// sit in registers, so k-direction taps cost no shared-memory loads; star stencils read
+// the i / j taps from the tile, cube stencils walk the (2R+1)^2 columns.  Float-float mode
+// converts the raw FP64 tile into float pairs in one pass before computing.
+#pragma once
+
+#include "sweep_kernel.cuh"
+
+namespace bk {
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(unsigned dst, const void *src) {
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ void store_stream(double *p, double v) { __stcs(p, v); }
+__device__ __forceinline__ void store_stream(float *p, float v) { __stcs(p, v); }
+__device__ __forceinline__ void store_stream(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+
+__device__ __forceinline__ float to_acc(__nv_bfloat16 x) { return __bfloat162float(x); }
+__device__ __forceinline__ float to_acc(float x) { return x; }
+__device__ __forceinline__ double to_acc(double x) { return x; }
+
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
+struct Sweep2Cfg {
+  static constexpr int ES = (int)sizeof(T);
+  static constexpr int VB = cmin(16, BI * ES);  // bytes per copy
+  static constexpr int VE = VB / ES;            // elements per copy
+  static constexpr int RP = (R + VE - 1) / VE * VE;  // i halo rounded up to whole copies
+  static constexpr int EK = BK + 2 * R, EJ = BJ + 2 * R, EI = BI + 2 * RP;
+  static constexpr int TILE = EK * EJ * EI;  // elements per brick tile
+  static constexpr int TILE_BYTES = (TILE * ES + 15) / 16 * 16;
+  static constexpr int TPB = BJ * BI;
+  // vectors of the neighbourhood (per brick)
+  static constexpr int NV_CENTRE = BK * BJ * (BI / VE);
+  static constexpr int NV_KF = R * BJ * (BI / VE);   // one k face
+  static constexpr int NV_JF = BK * R * (BI / VE);   // one j face
+  static constexpr int NV_IF = BK * BJ * (RP / VE);  // one i face
+  static constexpr int NV_STAR = NV_CENTRE + 2 * (NV_KF + NV_JF + NV_IF);
+  static constexpr int NV_CUBE = EK * EJ * (EI / VE);
+  static constexpr int NV = FAM == FAM_STAR ? NV_STAR : NV_CUBE;
+  static constexpr int EPT = (NV + TPB - 1) / TPB;  // plan entries per thread
+  // float-float keeps a converted float2 tile next to the raw buffers
+  static constexpr int FTILE_BYTES = ACC == ACCM_FF ? TILE * 8 : 0;
+  // bricks per CTA: as many as fit 128 threads and a ~100 KB shared-memory budget
+  static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 28 * 4;
+  static constexpr int NB = cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
+  static constexpr int NT = TPB * NB;
+  static constexpr int SMEM = NB * PER_BRICK;
+};
+
+// Tile coordinates (kk, jj, ii) of plan vector g for the star / cube neighbourhood.
+template <typename C, int BK, int BJ, int BI, int R, int FAM>
+__device__ __forceinline__ void plan_coords(int g, int &kk, int &jj, int &ii) {
+  constexpr int VE = C::VE, RP = C::RP;
+  if (FAM != FAM_STAR) {
+    constexpr int RV = C::EI / VE;
+    kk = g / (C::EJ * RV);
+    const int r = g - kk * (C::EJ * RV);
+    jj = r / RV;
+    ii = (r - jj * RV) * VE;
+    return;
+  }
+  constexpr int BV = BI / VE;
+  // regions: centre, k-lo, k-hi, j-lo, j-hi, i-lo, i-hi
+  if (g < C::NV_CENTRE) {
+    kk = g / (BJ * BV);
+    const int r = g - kk * (BJ * BV);
+    jj = r / BV;
+    ii = (r - jj * BV) * VE;
+    kk += R; jj += R; ii += RP;
+    return;
+  }
+  g -= C::NV_CENTRE;
+  if (g < 2 * C::NV_KF) {
+    const int hi = g >= C::NV_KF;
+    g -= hi * C::NV_KF;
+    kk = g / (BJ * BV);
+    const int r = g - kk * (BJ * BV);
+    jj = r / BV;
+    ii = (r - jj * BV) * VE;
+    kk += hi ? R + BK : 0; jj += R; ii += RP;
+    return;
+  }
+  g -= 2 * C::NV_KF;
+  if (g < 2 * C::NV_JF) {
+    const int hi = g >= C::NV_JF;
+    g -= hi * C::NV_JF;
+    kk = g / (R * BV);
+    const int r = g - kk * (R * BV);
+    jj = r / BV;
+    ii = (r - jj * BV) * VE;
+    kk += R; jj += hi ? R + BJ : 0; ii += RP;
+    return;
+  }
+  g -= 2 * C::NV_JF;
+  {
+    constexpr int IV = RP / VE;
+    const int hi = g >= C::NV_IF;
+    g -= hi * C::NV_IF;
+    kk = g / (BJ * IV);
+    const int r = g - kk * (BJ * IV);
+    jj = r / IV;
+    ii = (r - jj * IV) * VE;
+    kk += R; jj += R; ii += hi ? RP + BI : 0;
+  }
+}
+
+// Packed plan entry: slot (5 bits) | source element offset in the neighbour brick (13 bits)
+// | destination element offset in the tile (14 bits).  All three fit for bricks up to 8192
+// elements and tiles up to 16384 elements (checked on the host).
+template <typename C, int BK, int BJ, int BI, int R, int FAM>
+__device__ __forceinline__ unsigned plan_entry(int g) {
+  int kk, jj, ii;
+  plan_coords<C, BK, BJ, BI, R, FAM>(g, kk, jj, ii);
+  const int qk = kk < R ? -1 : (kk >= R + BK ? 1 : 0);
+  const int qj = jj < R ? -1 : (jj >= R + BJ ? 1 : 0);
+  const int qi = ii < C::RP ? -1 : (ii >= C::RP + BI ? 1 : 0);
+  const int lk = kk - R - qk * BK, lj = jj - R - qj * BJ, li = ii - C::RP - qi * BI;
+  const unsigned slot = (unsigned)((qk + 1) * 9 + (qj + 1) * 3 + (qi + 1));
+  const unsigned src = (unsigned)((lk * BJ + lj) * BI + li);
+  const unsigned dst = (unsigned)((kk * C::EJ + jj) * C::EI + ii);
+  return slot | (src << 5) | (dst << 18);
+}
+
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
+__global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC>::NT)
+sweep2_kernel(const SweepArgs a, const Taps tp) {
+  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
+  typedef typename Elem<T>::acc AT;
+  constexpr int TPB = C::TPB, NB = C::NB, EPT = C::EPT;
+  constexpr int EJ = C::EJ, EI = C::EI, SK = EJ * EI, SJ = EI, RP = C::RP;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
+  unsigned char *raw1 = smem_raw + NB * C::TILE_BYTES;          // [NB] tiles, buffer 1
+  float2 *ftiles = reinterpret_cast<float2 *>(smem_raw + 2 * NB * C::TILE_BYTES);
+  unsigned *nbrs = reinterpret_cast<unsigned *>(smem_raw + 2 * NB * C::TILE_BYTES + NB * C::FTILE_BYTES);
+  // nbrs: [3][NB][28]: adjacency of the groups being computed, copied and staged
+  // (three slots, so staging the group after next never overwrites one still read);
+  // entry [27] is the brick's active flag
+
+  const int slot = threadIdx.x / TPB, lt = threadIdx.x - slot * TPB;
+  const T *in = reinterpret_cast<const T *>(a.in) + a.in_off;
+  T *out = reinterpret_cast<T *>(a.out) + a.out_off;
+
+  unsigned plan[EPT];
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    const int g = e * TPB + lt;
+    plan[e] = g < C::NV ? plan_entry<C, BK, BJ, BI, R, FAM>(g) : 0xFFFFFFFFu;
+  }
+
+  const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
+
+  // stage the adjacency of group `grp` into nbrs[ns]
+  auto load_adj = [&](long long grp, int ns) {
+    unsigned *nbr = nbrs + (ns * NB + slot) * 28;
+    const long long n = grp * NB + slot;
+    for (int sl = lt; sl < 27; sl += TPB) {
+      unsigned v = 0;
+      int ok = 0;
+      if (grp < ngroups && n < a.nlist) {
+        const unsigned b = a.blist[n];
+        if (b < a.nbricks) {
+          v = a.adj[(size_t)b * 27 + sl];
+          ok = 1;
+          if (sl == 13 && ((long long)v >= a.out_chunks || (long long)v >= a.in_chunks)) ok = 0;
+          if ((long long)v >= a.in_chunks || !ok) { atomicOr(a.err, FLAG_BOUNDS); v = 0; }
+        } else if (sl == 13) {
+          atomicOr(a.err, FLAG_BOUNDS);
+        }
+      }
+      nbr[sl] = v;
+      if (sl == 13) nbr[27] = ok;
+    }
+  };
+  // issue the asynchronous gather of the group staged in nbrs[ns] into raw buffer buf
+  auto issue = [&](int buf, int ns) {
+    const unsigned *nbr = nbrs + (ns * NB + slot) * 28;
+    if (nbr[27]) {
+      unsigned char *tile = (buf ? raw1 : raw0) + slot * C::TILE_BYTES;
+      const unsigned tbase = smem_u32(tile);
+#pragma unroll
+      for (int e = 0; e < EPT; ++e) {
+        const unsigned p = plan[e];
+        if (p != 0xFFFFFFFFu) {
+          const unsigned sl = p & 31u, src = (p >> 5) & 8191u, dst = p >> 18;
+          const T *g = in + (size_t)nbr[sl] * a.in_step + src;
+          cp_async<C::VB>(tbase + dst * C::ES, g);
+        }
+      }
+    }
+    cp_async_commit();
+  };
+
+  long long grp = blockIdx.x;
+  load_adj(grp, 0);
+  __syncthreads();
+  issue(0, 0);
+
+  for (int it = 0; grp < ngroups; grp += gridDim.x, ++it) {
+    const int cur = it & 1, nxt = cur ^ 1;
+    const int ncur = it % 3, nnxt = (it + 1) % 3;
+    load_adj(grp + gridDim.x, nnxt);
+    __syncthreads();  // nbrs[nnxt] visible; every thread is done with raw[nxt]
+    issue(nxt, nnxt);
+    cp_async_wait<1>();  // this thread's copies for the current group have landed
+    __syncthreads();     // ... and everybody else's
+
+    const unsigned *nbr = nbrs + (ncur * NB + slot) * 28;
+    const bool active = nbr[27] != 0;
+    const T *rt = reinterpret_cast<const T *>((cur ? raw1 : raw0) + slot * C::TILE_BYTES);
+    if constexpr (ACC == ACCM_FF) {
+      // one pass: raw doubles -> float pairs
+      float2 *ft = ftiles + slot * C::TILE;
+      if (active)
+        for (int e = lt; e < C::TILE; e += TPB) ft[e] = split_f64(reinterpret_cast<const double *>(rt)[e]);
+      __syncthreads();
+    }
+    if (active) {
+      const int j = lt / BI, i = lt - (lt / BI) * BI;
+      T *ob = out + (size_t)nbr[13] * a.out_step + (size_t)(j * BI + i);
+      const int cofs = (j + R) * SJ + (i + RP);  // column (j, i) at kk = 0
+      if constexpr (ACC == ACCM_FF) {
+        const float2 *ft = ftiles + slot * C::TILE;
+        if constexpr (FAM == FAM_STAR) {
+          float2 w[BK + 2 * R];
+#pragma unroll
+          for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = ft[kk * SK + cofs];
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            const float2 *c = ft + (k + R) * SK + cofs;
+            FFAcc acc;
+            acc.first(tp.cf[0], tp.cl[0], w[k + R]);
+#pragma unroll
+            for (int d = 1; d <= R; ++d) {
+              const int t = 1 + 6 * (d - 1);
+              acc.add(tp.cf[t + 0], tp.cl[t + 0], c[d]);
+              acc.add(tp.cf[t + 1], tp.cl[t + 1], c[-d]);
+              acc.add(tp.cf[t + 2], tp.cl[t + 2], c[d * SJ]);
+              acc.add(tp.cf[t + 3], tp.cl[t + 3], c[-d * SJ]);
+              acc.add(tp.cf[t + 4], tp.cl[t + 4], w[k + R + d]);
+              acc.add(tp.cf[t + 5], tp.cl[t + 5], w[k + R - d]);
+              acc.renorm();
+            }
+            store_stream(ob + k * BJ * BI, acc.result());
+          }
+        } else if constexpr (FAM == FAM_CUBE) {
+          FFAcc acc[BK];
+#pragma unroll
+          for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+            for (int di = -R; di <= R; ++di) {
+              float2 w[BK + 2 * R];
+#pragma unroll
+              for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = ft[kk * SK + cofs + dj * SJ + di];
+#pragma unroll
+              for (int k = 0; k < BK; ++k) {
+#pragma unroll
+                for (int dk = -R; dk <= R; ++dk) {
+                  const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+                  if (dj == -R && di == -R && dk == -R) acc[k].first(tp.cf[t], tp.cl[t], w[k + R + dk]);
+                  else acc[k].add(tp.cf[t], tp.cl[t], w[k + R + dk]);
+                }
+                acc[k].renorm();
+              }
+            }
+#pragma unroll
+          for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k].result());
+        } else {
+#pragma unroll 1
+          for (int k = 0; k < BK; ++k) {
+            const float2 *c = ft + (k + R) * SK + cofs;
+            FFAcc acc;
+            acc.first(tp.cf[0], tp.cl[0], c[tp.toff[0]]);
+            for (int t = 1; t < tp.n; ++t) {
+              acc.add(tp.cf[t], tp.cl[t], c[tp.toff[t]]);
+              if ((t & 7) == 7) acc.renorm();
+            }
+            store_stream(ob + k * BJ * BI, acc.result());
+          }
+        }
+      } else {
+        if constexpr (FAM == FAM_STAR) {
+          AT w[BK + 2 * R];
+#pragma unroll
+          for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = to_acc(rt[kk * SK + cofs]);
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            const T *c = rt + (k + R) * SK + cofs;
+            AT v;
+            if constexpr (ACC == ACCM_NATIVE) {
+              v = coef<AT>(tp, 0) * w[k + R];
+#pragma unroll
+              for (int d = 1; d <= R; ++d) {
+                const int t = 1 + 6 * (d - 1);
+                v = fma(coef<AT>(tp, t + 0), to_acc(c[d]), v);
+                v = fma(coef<AT>(tp, t + 1), to_acc(c[-d]), v);
+                v = fma(coef<AT>(tp, t + 2), to_acc(c[d * SJ]), v);
+                v = fma(coef<AT>(tp, t + 3), to_acc(c[-d * SJ]), v);
+                v = fma(coef<AT>(tp, t + 4), w[k + R + d], v);
+                v = fma(coef<AT>(tp, t + 5), w[k + R - d], v);
+              }
+            } else {
+              AT row = coef<AT>(tp, 0) * w[k + R];
+#pragma unroll
+              for (int d = 1; d <= R; ++d) {
+                const int t = 1 + 6 * (d - 1);
+                row = fma(coef<AT>(tp, t + 0), to_acc(c[d]), row);
+                row = fma(coef<AT>(tp, t + 1), to_acc(c[-d]), row);
+              }
+              AT s = row, comp = AT(0);
+#pragma unroll
+              for (int d = 1; d <= R; ++d) {
+                const int t = 1 + 6 * (d - 1);
+                neumaier(s, comp, coef<AT>(tp, t + 2) * to_acc(c[d * SJ]));
+                neumaier(s, comp, coef<AT>(tp, t + 3) * to_acc(c[-d * SJ]));
+                neumaier(s, comp, coef<AT>(tp, t + 4) * w[k + R + d]);
+                neumaier(s, comp, coef<AT>(tp, t + 5) * w[k + R - d]);
+              }
+              v = s + comp;
+            }
+            store_stream(ob + k * BJ * BI, v);
+          }
+        } else if constexpr (FAM == FAM_CUBE) {
+          AT acc[BK], comp[BK];
+#pragma unroll
+          for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+            for (int di = -R; di <= R; ++di) {
+              AT w[BK + 2 * R];
+#pragma unroll
+              for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = to_acc(rt[kk * SK + cofs + dj * SJ + di]);
+#pragma unroll
+              for (int k = 0; k < BK; ++k) {
+                if constexpr (ACC == ACCM_NATIVE) {
+#pragma unroll
+                  for (int dk = -R; dk <= R; ++dk) {
+                    const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+                    if (dj == -R && di == -R && dk == -R) acc[k] = coef<AT>(tp, t) * w[k + R + dk];
+                    else acc[k] = fma(coef<AT>(tp, t), w[k + R + dk], acc[k]);
+                  }
+                } else {
+                  // the 2R+1 k taps of this column as one FMA chain, columns Neumaier-summed
+                  const int t0 = ((0) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+                  AT col = coef<AT>(tp, t0) * w[k];
+#pragma unroll
+                  for (int dk = -R + 1; dk <= R; ++dk) {
+                    const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+                    col = fma(coef<AT>(tp, t), w[k + R + dk], col);
+                  }
+                  if (dj == -R && di == -R) {
+                    acc[k] = col;
+                    comp[k] = AT(0);
+                  } else {
+                    neumaier(acc[k], comp[k], col);
+                  }
+                }
+              }
+            }
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            if constexpr (ACC == ACCM_NATIVE) store_stream(ob + k * BJ * BI, acc[k]);
+            else store_stream(ob + k * BJ * BI, acc[k] + comp[k]);
+          }
+        } else {
+#pragma unroll 1
+          for (int k = 0; k < BK; ++k) {
+            const T *c = rt + (k + R) * SK + cofs;
+            AT v;
+            if constexpr (ACC == ACCM_NATIVE) {
+              v = coef<AT>(tp, 0) * to_acc(c[tp.toff[0]]);
+              for (int t = 1; t < tp.n; ++t) v = fma(coef<AT>(tp, t), to_acc(c[tp.toff[t]]), v);
+            } else {
+              AT s = coef<AT>(tp, 0) * to_acc(c[tp.toff[0]]), comp = AT(0);
+              for (int t = 1; t < tp.n; ++t) neumaier(s, comp, coef<AT>(tp, t) * to_acc(c[tp.toff[t]]));
+              v = s + comp;
+            }
+            store_stream(ob + k * BJ * BI, v);
+          }
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();  // no copy may outlive the kernel
+}
+
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
+int launch_sweep2(const SweepArgs &a, const Taps &tp, cudaStream_t s) {
+  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
+  static_assert(C::SMEM <= 227 * 1024, "tile too large");
+  static_assert(BK * BJ * BI <= 8192 && C::TILE <= 16384, "plan entry fields overflow");
+  auto kern = sweep2_kernel<T, BK, BJ, BI, R, FAM, ACC>;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess && C::SMEM > 48 * 1024)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, C::SMEM);
+  if (e != cudaSuccess) return cuda_fail(e, "sweep2 launch setup");
+  if (per_sm < 1) return fail(BK_ERR_UNSUPPORTED, "sweep2 kernel does not fit on an SM");
+  const long long groups = ((long long)a.nlist + C::NB - 1) / C::NB;
+  long long grid = (long long)sms * per_sm;
+  if (grid > groups) grid = groups;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, C::NT, C::SMEM, s>>>(a, tp);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "sweep2 kernel launch");
+  return BK_OK;
+}
+
+// Tile geometry the host needs for generic-family tap offsets.
+template <typename T, int BK, int BJ, int BI, int R>
+struct Sweep2Geom {
+  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM_GENERIC, ACCM_NATIVE> C;
+  static constexpr int EJ = C::EJ, EI = C::EI;
+};
+
+}  // namespace bk

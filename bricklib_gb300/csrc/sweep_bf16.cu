@@ -1,5 +1,5 @@
-// Instantiations of the sweep kernel for __nv_bfloat16 storage.
-#include "sweep_kernel.cuh"
+// Instantiations of the sweep kernels for __nv_bfloat16 storage.
+#include "sweep2_kernel.cuh"
 
 namespace bk {
 
@@ -16,7 +16,42 @@ namespace bk {
   BK_CASE(BK_, BJ_, BI_, 4, FAM_GENERIC, true, ACC_) \
   BK_CASE(BK_, BJ_, BI_, 4, FAM_GENERIC, false, ACC_)
 
-int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s) {
+// pipelined kernel (row-major layouts, aligned fields); the generic family's tap offsets
+// are rebased onto that kernel's padded tile
+#define BK_CASE2(BK_, BJ_, BI_, R_, FAM_, ACC_)                                         \
+  if (p.r == R_ && p.fam == FAM_ && p.acc == ACC_) {                                    \
+    if (FAM_ == FAM_GENERIC) {                                                          \
+      typedef Sweep2Geom<__nv_bfloat16, BK_, BJ_, BI_, R_> G;                                     \
+      for (int t = 0; t < tp.n; ++t)                                                    \
+        tp.toff[t] = (p.offs[t][0] * G::EJ + p.offs[t][1]) * G::EI + p.offs[t][2];      \
+    }                                                                                   \
+    return launch_sweep2<__nv_bfloat16, BK_, BJ_, BI_, R_, FAM_, ACC_>(a, tp, s);                 \
+  }
+
+#define BK_SHAPE_SET2(BK_, BJ_, BI_, ACC_)   \
+  BK_CASE2(BK_, BJ_, BI_, 1, FAM_STAR, ACC_) \
+  BK_CASE2(BK_, BJ_, BI_, 2, FAM_STAR, ACC_) \
+  BK_CASE2(BK_, BJ_, BI_, 4, FAM_STAR, ACC_) \
+  BK_CASE2(BK_, BJ_, BI_, 1, FAM_CUBE, ACC_) \
+  BK_CASE2(BK_, BJ_, BI_, 2, FAM_CUBE, ACC_) \
+  BK_CASE2(BK_, BJ_, BI_, 4, FAM_GENERIC, ACC_)
+
+int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
+  if (p.v2) {
+    if (p.shape == 0) {
+      BK_SHAPE_SET2(8, 8, 8, ACCM_NATIVE)
+      BK_SHAPE_SET2(8, 8, 8, ACCM_COMP)
+    } else if (p.shape == 1) {
+      BK_SHAPE_SET2(4, 4, 4, ACCM_NATIVE)
+    } else if (p.shape == 2) {
+      BK_SHAPE_SET2(16, 8, 8, ACCM_NATIVE)
+    } else if (p.shape == 3) {
+      BK_SHAPE_SET2(8, 8, 32, ACCM_NATIVE)
+    }
+  }
+  // the generic family of the one-shot kernel uses the host-computed offsets
+  if (p.fam == FAM_GENERIC)
+    for (int t = 0; t < tp.n; ++t) tp.toff[t] = p.toff1[t];
   if (p.shape == 0) {
     BK_SHAPE_SET(8, 8, 8, ACCM_NATIVE)
     BK_SHAPE_SET(8, 8, 8, ACCM_COMP)

@@ -401,13 +401,16 @@ struct SweepPlan {
   int dtype;
   int shape;  // 0: 8x8x8, 1: 4x4x4, 2: 16x8x8, 3: 8x8x32
   bool rm;
+  bool v2;    // row-major and aligned: the pipelined kernel applies
   int fam;
   int r;
   int acc;
+  const int (*offs)[3];  // tap offsets in kernel order (generic family)
+  const int *toff1;      // generic-family tile offsets for the one-shot kernel
 };
 
-int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s);
-int sweep_dispatch_f32(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s);
-int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, const Taps &tp, cudaStream_t s);
+int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
+int sweep_dispatch_f32(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
+int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
 
 }  // namespace bk

@@ -22,6 +22,17 @@ GOLD = os.path.join(os.path.dirname(__file__), "golden")
 TOL64 = 1e-12
 
 
+@pytest.fixture(params=["pipelined", "oneshot"])
+def kernel(request, monkeypatch):
+    """Row-major aligned sweeps run the pipelined kernel; BK_SWEEP_ONESHOT=1 selects the
+    one-shot kernel that also serves every other layout.  Both must pass."""
+    if request.param == "oneshot":
+        monkeypatch.setenv("BK_SWEEP_ONESHOT", "1")
+    else:
+        monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+    return request.param
+
+
 def mixed_ok(a, b, tol=TOL64):
     d = np.abs(a - b)
     return bool(np.all((d < tol) | (d < (np.abs(a) + np.abs(b)) * tol))), float(d.max(initial=0))
@@ -64,7 +75,7 @@ def test_fp64_matches_reference_golden(path):
 
 
 @pytest.mark.parametrize("name", stencils.PLAIN_SHAPES + ("heat7", "lap7"))
-def test_fp64_matches_oracle_64(name):
+def test_fp64_matches_oracle_64(name, kernel):
     st = stencils.make(name, 7)
     dom, arr, got = device_sweep(64, st, seed=42)
     ok, md = mixed_ok(got, oracle_array(dom, arr, st))
@@ -77,7 +88,7 @@ LAYOUTS = [((8, 8, 8), (1, 1, 8)), ((8, 8, 8), (1, 2, 2)), ((8, 8, 8), (2, 4, 4)
 
 @pytest.mark.parametrize("bdim,fold", LAYOUTS, ids=lambda x: "x".join(map(str, x)))
 @pytest.mark.parametrize("name", ["star7", "star13", "cube27", "cube125"])
-def test_fp64_layouts(bdim, fold, name):
+def test_fp64_layouts(bdim, fold, name, kernel):
     st = stencils.make(name, 3)
     if st.radius > min(bdim):
         pytest.skip("radius beyond the brick")
@@ -88,7 +99,7 @@ def test_fp64_layouts(bdim, fold, name):
     assert ok, f"max |diff| {md}"
 
 
-def test_generic_family_19pt():
+def test_generic_family_19pt(kernel):
     taps = [t for t in stencils.cube_taps(1)[0] if sum(1 for a in t if a) <= 2]
     st = stencils.custom("d3pt19", taps, stencils.uniform(5, len(taps), 0, 1))
     assert B.stencil_family(st)[1] == 0
@@ -99,7 +110,7 @@ def test_generic_family_19pt():
 
 @pytest.mark.parametrize("name", stencils.PLAIN_SHAPES)
 @pytest.mark.parametrize("acc", [BK_ACC_NATIVE, BK_ACC_COMPENSATED])
-def test_fp32_against_fp64_oracle(name, acc):
+def test_fp32_against_fp64_oracle(name, acc, kernel):
     st = stencils.make(name, 11)
     dom, arr, got = device_sweep(64, st, dtype=BK_F32, acc=acc, seed=5)
     ref = oracle_array(dom, arr.astype(np.float32).astype(np.float64), st)
@@ -116,7 +127,7 @@ def test_compensated_beats_native_on_cube125():
 
 
 @pytest.mark.parametrize("name", ["star7", "cube125"])
-def test_bf16_against_fp64_oracle(name):
+def test_bf16_against_fp64_oracle(name, kernel):
     st = stencils.make(name, 4)
     dom, arr, got = device_sweep(32, st, dtype=BK_BF16, acc=BK_ACC_COMPENSATED, seed=6)
     arr_b = B.bf16_to_f32(B.f32_to_bf16(arr.astype(np.float32))).astype(np.float64)
@@ -221,7 +232,7 @@ def test_empty_brick_list_is_a_no_op():
 
 
 @pytest.mark.parametrize("name", stencils.PLAIN_SHAPES + ("heat7", "lap7"))
-def test_fp64_floatfloat_against_oracle(name):
+def test_fp64_floatfloat_against_oracle(name, kernel):
     """FP64 storage computed in float-float on the FP32 pipes: normwise error against the
     FP64 oracle within 1e-12 (47-bit inputs and Dot2 accumulation give ~1e-14)."""
     st = stencils.make(name, 7)
