@@ -46,13 +46,44 @@ __device__ __forceinline__ double to_acc(double x) { return x; }
 __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
+// Smallest row length >= need (a multiple of ve) for which the 32/bi consecutive rows
+// read by one warp map to pairwise disjoint bank sets (8-byte elements: per half warp).
+__host__ __device__ constexpr bool rows_disjoint(int ei, int bi, int es) {
+  const int words_row = ei * es / 4 > 0 ? ei * es / 4 : 1;  // row stride in 4-byte words
+  const int seg = (bi * es + 3) / 4;                          // words one row segment covers
+  const int lanes = es == 8 ? 16 : 32;
+  const int rows = lanes / bi > 0 ? lanes / bi : 1;
+  if (seg * rows > 32) return true;  // the warp needs several wavefronts whatever the stride
+  for (int a = 0; a < rows; ++a)
+    for (int b = a + 1; b < rows; ++b)
+      for (int x = 0; x < seg; ++x)
+        for (int y = 0; y < seg; ++y)
+          if ((a * words_row + x) % 32 == (b * words_row + y) % 32) return false;
+  return true;
+}
+__host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, int ve) {
+  int ei = need;
+  for (int t = 0; t < 64; ++t, ei += ve)
+    if (rows_disjoint(ei, bi, es)) return ei;
+  return need;
+}
+
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
 struct Sweep2Cfg {
   static constexpr int ES = (int)sizeof(T);
   static constexpr int VB = cmin(16, BI * ES);  // bytes per copy
   static constexpr int VE = VB / ES;            // elements per copy
   static constexpr int RP = (R + VE - 1) / VE * VE;  // i halo rounded up to whole copies
-  static constexpr int EK = BK + 2 * R, EJ = BJ + 2 * R, EI = BI + 2 * RP;
+  static constexpr int EK = BK + 2 * R, EJ = BJ + 2 * R;
+  // Tile row length, at least BI + 2*RP, chosen against shared-memory bank conflicts.
+  // 8-byte elements in 8-wide rows: a half warp reads two rows; lanes are assigned to
+  // rows in the order 0,2,1,3 so those two rows are two apart, and a row length of
+  // 4 (mod 8) elements puts them 16 banks apart.  Otherwise: pad until the rows one warp
+  // reads fall in disjoint banks.
+  static constexpr bool PERM = ES == 8 && BI == 8;
+  static constexpr int NEED = BI + 2 * RP;
+  static constexpr int EI = PERM ? (NEED % 8 <= 4 ? NEED - NEED % 8 + 4 : NEED - NEED % 8 + 12)
+                                 : conflict_free_row(NEED, BI, ES, VE);
   static constexpr int TILE = EK * EJ * EI;  // elements per brick tile
   static constexpr int TILE_BYTES = (TILE * ES + 15) / 16 * 16;
   static constexpr int TPB = BJ * BI;
@@ -62,11 +93,11 @@ struct Sweep2Cfg {
   static constexpr int NV_JF = BK * R * (BI / VE);   // one j face
   static constexpr int NV_IF = BK * BJ * (RP / VE);  // one i face
   static constexpr int NV_STAR = NV_CENTRE + 2 * (NV_KF + NV_JF + NV_IF);
-  static constexpr int NV_CUBE = EK * EJ * (EI / VE);
+  static constexpr int NV_CUBE = EK * EJ * (NEED / VE);  // the row padding is never fetched
   static constexpr int NV = FAM == FAM_STAR ? NV_STAR : NV_CUBE;
   static constexpr int EPT = (NV + TPB - 1) / TPB;  // plan entries per thread
-  // float-float keeps a converted float2 tile next to the raw buffers
-  static constexpr int FTILE_BYTES = ACC == ACCM_FF ? TILE * 8 : 0;
+  // float-float converts each raw FP64 tile into float pairs in place (same 8 bytes)
+  static constexpr int FTILE_BYTES = 0;
   // bricks per CTA: as many as fit 128 threads and a ~100 KB shared-memory budget
   static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 28 * 4;
   static constexpr int NB = cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
@@ -79,7 +110,7 @@ template <typename C, int BK, int BJ, int BI, int R, int FAM>
 __device__ __forceinline__ void plan_coords(int g, int &kk, int &jj, int &ii) {
   constexpr int VE = C::VE, RP = C::RP;
   if (FAM != FAM_STAR) {
-    constexpr int RV = C::EI / VE;
+    constexpr int RV = C::NEED / VE;
     kk = g / (C::EJ * RV);
     const int r = g - kk * (C::EJ * RV);
     jj = r / RV;
@@ -159,7 +190,6 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
   unsigned char *raw1 = smem_raw + NB * C::TILE_BYTES;          // [NB] tiles, buffer 1
-  float2 *ftiles = reinterpret_cast<float2 *>(smem_raw + 2 * NB * C::TILE_BYTES);
   unsigned *nbrs = reinterpret_cast<unsigned *>(smem_raw + 2 * NB * C::TILE_BYTES + NB * C::FTILE_BYTES);
   // nbrs: [3][NB][28]: adjacency of the groups being computed, copied and staged
   // (three slots, so staging the group after next never overwrites one still read);
@@ -237,18 +267,20 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     const bool active = nbr[27] != 0;
     const T *rt = reinterpret_cast<const T *>((cur ? raw1 : raw0) + slot * C::TILE_BYTES);
     if constexpr (ACC == ACCM_FF) {
-      // one pass: raw doubles -> float pairs
-      float2 *ft = ftiles + slot * C::TILE;
+      // one pass, in place: raw doubles -> float pairs (each thread its own elements)
+      float2 *ft = reinterpret_cast<float2 *>(const_cast<T *>(rt));
       if (active)
         for (int e = lt; e < C::TILE; e += TPB) ft[e] = split_f64(reinterpret_cast<const double *>(rt)[e]);
       __syncthreads();
     }
     if (active) {
-      const int j = lt / BI, i = lt - (lt / BI) * BI;
+      int j = lt / BI;
+      const int i = lt - j * BI;
+      if (C::PERM) j = (j & ~3) | ((j & 1) << 1) | ((j >> 1) & 1);  // rows 0,2,1,3 per warp
       T *ob = out + (size_t)nbr[13] * a.out_step + (size_t)(j * BI + i);
       const int cofs = (j + R) * SJ + (i + RP);  // column (j, i) at kk = 0
       if constexpr (ACC == ACCM_FF) {
-        const float2 *ft = ftiles + slot * C::TILE;
+        const float2 *ft = reinterpret_cast<const float2 *>(rt);
         if constexpr (FAM == FAM_STAR) {
           float2 w[BK + 2 * R];
 #pragma unroll
