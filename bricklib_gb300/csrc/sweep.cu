@@ -129,6 +129,11 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
     const size_t ve = vb / es;
     plan->v2 = plan->rm && (reinterpret_cast<uintptr_t>(in->dat) % 16 == 0) && in->step % ve == 0 &&
                in->offset % ve == 0 && !getenv("BK_SWEEP_ONESHOT");
+    // float-float cubes and the radius-4 star are bound by the FP32 pipes; the one-shot
+    // kernel's single tile buffer keeps twice as many CTAs resident and wins there
+    // (measured on GB300: cube125 18.6 vs 12.8, cube27 61 vs 46, star25 17 vs 15 GStencil/s)
+    if (plan->acc == ACCM_FF && (plan->fam == FAM_CUBE || plan->r >= 4) && !getenv("BK_SWEEP_PIPELINED"))
+      plan->v2 = false;
   }
   int *err = device_error_word();
   if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");

@@ -140,7 +140,10 @@ int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, in
  *   blist      device list of nlist brick indices to compute (e.g. the interior bricks
  *              grid[GB..STRIDEB-GB)^3 of 3axis.cu:167)
  * Neighbour or list indices >= chunks/nbricks are clamped to brick 0 and reported by
- * bk_error_flags() as BK_ERR_BOUNDS; the kernel never reads outside the storage. */
+ * bk_error_flags() as BK_ERR_BOUNDS; the kernel never reads outside the storage.
+ * Two kernels implement it: a pipelined one (row-major layouts, 16-byte aligned input)
+ * and a one-shot one (everything).  The environment variables BK_SWEEP_ONESHOT=1 and
+ * BK_SWEEP_PIPELINED=1 override the built-in choice (used by the parity tests). */
 int bk_sweep(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
              const unsigned *blist, unsigned nlist, const bk_stencil *st, const bk_layout *lay,
              int acc, void *stream);

@@ -24,12 +24,15 @@ TOL64 = 1e-12
 
 @pytest.fixture(params=["pipelined", "oneshot"])
 def kernel(request, monkeypatch):
-    """Row-major aligned sweeps run the pipelined kernel; BK_SWEEP_ONESHOT=1 selects the
-    one-shot kernel that also serves every other layout.  Both must pass."""
+    """Row-major aligned sweeps run the pipelined kernel (BK_SWEEP_PIPELINED=1 forces it where
+    the one-shot kernel is preferred); BK_SWEEP_ONESHOT=1 selects the one-shot kernel that
+    also serves every other layout.  Both must pass."""
     if request.param == "oneshot":
         monkeypatch.setenv("BK_SWEEP_ONESHOT", "1")
+        monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
     else:
         monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+        monkeypatch.setenv("BK_SWEEP_PIPELINED", "1")
     return request.param
 
 
