@@ -459,3 +459,30 @@ def timeSteps(a: Brick, b: Brick, blist: BrickList, st, steps: int, plan: Option
          C.byref(cst), C.byref(a.layout.to_c()), acc, steps, fill_every if plan else 0, 1 if use_graph else 0,
          stream_ptr(stream))
     return a if steps % 2 == 0 else b
+
+
+# ------------------------------------------------------------------ precision form
+
+def convertField(src: Brick, dst: Brick, blist: BrickList, stream=None) -> None:
+    """Element-wise storage-type conversion of the listed bricks (bk_convert)."""
+    call("bk_convert", C.byref(src.field()), C.byref(dst.field()), C.c_void_p(blist.ptr), blist.n,
+         C.byref(src.layout.to_c()), stream_ptr(stream))
+
+
+def fieldNorms(a: Brick, ref: Brick, blist: BrickList, stream=None) -> dict:
+    """FP64 device reduction of the error of field a against ref (bk_field_norms)."""
+    out = (C.c_double * 4)()
+    call("bk_field_norms", C.byref(a.field()), C.byref(ref.field()), C.c_void_p(blist.ptr), blist.n,
+         C.byref(a.layout.to_c()), stream_ptr(stream), out)
+    n = blist.n * a.layout.size
+    return {"max_abs": out[0], "sum_sq": out[1], "max_ref": out[2], "sum_sq_ref": out[3],
+            "rms": (out[1] / n) ** 0.5 if n else 0.0,
+            "max_rel": out[0] / out[2] if out[2] else 0.0,
+            "rms_rel": (out[1] / out[3]) ** 0.5 if out[3] else 0.0}
+
+
+def fillSines(brick: Brick, grid_bricks, ghost_bricks, nwaves: int = 8, seed: int = 0, noise: float = 1e-3,
+              stream=None) -> None:
+    """The seeded sum-of-sines initial field on every brick of an init_grid layout."""
+    call("bk_fill_sines", C.byref(brick.field()), C.byref(brick.layout.to_c()), (C.c_long * 3)(*grid_bricks),
+         (C.c_long * 3)(*ghost_bricks), nwaves, seed, noise, stream_ptr(stream))

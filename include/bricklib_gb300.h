@@ -174,6 +174,29 @@ int bk_periodic_plan(const unsigned *grid, const long nb[3], const long gb[3], u
  * nlinks {from, to, bytes} triples (uint64 each); bytes must be a multiple of 8. */
 int bk_region_copy(const uint64_t *links, unsigned nlinks, void *stream);
 
+/* ------------------------------------------------------------------ precision form */
+
+/* Element-wise conversion of the listed bricks of field src into field dst (any pair of
+ * storage types; round to nearest even).  Used to start FP32 / BF16 runs from the same
+ * values as an FP64 run. */
+int bk_convert(const bk_field *src, const bk_field *dst, const unsigned *blist, unsigned nlist,
+               const bk_layout *lay, void *stream);
+
+/* FP64 error norms of field a against field ref over the listed bricks, reduced on the
+ * device in FP64: out[0] = max |a - ref|, out[1] = sum (a - ref)^2, out[2] = max |ref|,
+ * out[3] = sum ref^2.  Synchronises the stream.  Its partial sums live in a device buffer
+ * the library allocates on the first call per device and keeps until exit. */
+int bk_field_norms(const bk_field *a, const bk_field *ref, const unsigned *blist, unsigned nlist,
+                   const bk_layout *lay, void *stream, double out[4]);
+
+/* Seeded initial field: the sum of `nwaves` sines with integer wave numbers in 1..4 and
+ * random phases on the periodic interior, plus `noise` times uniform[-1,1) noise, written
+ * to every brick of an init_grid layout of grid_bricks (k,j,i) bricks with ghost_bricks
+ * ghost bricks per side (brick index = linear grid position).  Ghost bricks receive the
+ * periodic continuation.  Evaluated in FP32 and stored in the field's type. */
+int bk_fill_sines(const bk_field *f, const bk_layout *lay, const long grid_bricks[3],
+                  const long ghost_bricks[3], int nwaves, uint64_t seed, double noise, void *stream);
+
 /* ------------------------------------------------------------------ time steps */
 
 /* T time steps, ping-pong between fields a and b (weak/main.cu:277-282): before every
