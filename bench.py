@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-alt", action="store_true")
+    p.add_argument("--form", default="plain", choices=["plain", "precision"],
+                   help="plain: the FP64 drop-in bench line; precision: the precision-form error study")
     return p.parse_args()
 
 
@@ -394,9 +396,28 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """The precision form (FP64 / FP32 / BF16 storage, 1, 10, 100 steps): one JSON line with
+    the max and RMS error of every run against the FP64 run, per stencil and step count."""
+    import torch
+    from bricklib_gb300 import precision
+    from bricklib_gb300._abi import call
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    call("bk_set_device", local)
+    t = time.perf_counter()
+    recs = precision.run_study(n=args.n, shapes=("heat7", "cube125"), variants=("f32", "bf16", "f64-floatfloat"),
+                               steps=(1, 10, 100), stream=torch.cuda.current_stream().cuda_stream)
+    if rank == 0:
+        print(json.dumps({"form": "precision", "n": args.n, "seconds": round(time.perf_counter() - t, 1),
+                          "reference": "FP64 native run on the device", "records": recs}), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.form == "precision":
+        run_precision(a)
     else:
         run_ours(a)

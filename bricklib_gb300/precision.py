@@ -56,7 +56,6 @@ def run_study(n: int = 512, shapes: Iterable[str] = ("heat7", "cube125"),
     run at each checkpoint in `steps`.  Returns one record per (shape, variant, steps)."""
     steps = sorted(set(int(s) for s in steps))
     ref = PeriodicProblem(n, BK_F64)
-    snap = PeriodicProblem(n, BK_F64)  # FP64 result at the current checkpoint
     out: List[Dict] = []
     for shape in shapes:
         st = B.to_c_stencil(stencils.make(shape, 5))
@@ -90,5 +89,4 @@ def run_study(n: int = 512, shapes: Iterable[str] = ("heat7", "cube125"),
                     rec["gstencil_s_incl_fill"] = round(todo * n ** 3 / dt_s / 1e9, 2)
                 out.append(rec)
             done = t
-    del snap
     return out
