@@ -73,6 +73,8 @@ SIGNATURES = {
     "bk_convert": (C.c_int, [_P(bk_field), _P(bk_field), _vp, C.c_uint, _P(bk_layout), _vp]),
     "bk_field_norms": (C.c_int, [_P(bk_field), _P(bk_field), _vp, C.c_uint, _P(bk_layout), _vp,
                                  _P(C.c_double)]),
+    "bk_field_norms_noalloc": (C.c_int, [_P(bk_field), _P(bk_field), _vp, C.c_uint, _P(bk_layout), _vp,
+                                         _P(C.c_double)]),
     "bk_fill_sines": (C.c_int, [_P(bk_field), _P(bk_layout), _P(C.c_long), _P(C.c_long), C.c_int, C.c_uint64,
                                 C.c_double, _vp]),
     "bk_steps": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_field), _vp, C.c_uint, _vp, C.c_uint,

@@ -328,3 +328,99 @@ int bk_fill_sines(const bk_field *f, const bk_layout *lay, const long grid_brick
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Norms without allocation.
+//
+// Some callers cannot call cudaMalloc: a serving loop with a latency budget (cudaMalloc and
+// cudaFree can synchronise the device and stall every stream) or a process whose device
+// memory is all reserved up front by another allocator.  bk_field_norms_noalloc gives them
+// the FP64 error norms with no allocation at all: its scratch -- one partial per listed
+// brick, the 4-double result and an error word -- is the file-scope array below, which every
+// GPU that loads this library holds until the process exits.  All calls share it and it
+// keeps the last call's contents; calls whose work overlaps on the GPU (on different
+// streams, or from several host threads) race on it.
+namespace bk {
+
+constexpr int NOALLOC_MAX_BRICKS = BK_NORMS_NOALLOC_MAX_BRICKS;
+// [0, MAX): per-brick partials; [MAX]: result (x, y, z, w); [MAX + 1].x: error word
+static __device__ __align__(256) double4 g_noalloc_scratch[NOALLOC_MAX_BRICKS + 2];
+
+static std::mutex g_noalloc_mu;
+static std::vector<double4 *> g_noalloc_addr;  // device address of the array, per device
+
+// Device address of g_noalloc_scratch for the current device (looked up once per device,
+// with that device current; the host-side name of the array is not a device address).
+static int noalloc_scratch(double4 **p) {
+  int dev = 0;
+  BK_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if ((int)g_noalloc_addr.size() <= dev) g_noalloc_addr.resize(dev + 1, nullptr);
+  if (!g_noalloc_addr[dev]) {
+    void *addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_addr[dev] = reinterpret_cast<double4 *>(addr);
+  }
+  *p = g_noalloc_addr[dev];
+  return BK_OK;
+}
+
+// One partial-norm block per listed brick, then one final block over those partials.
+template <typename A, typename Rt>
+int launch_norms_per_brick(const bk_field *a, const bk_field *r, const unsigned *blist, unsigned nlist, int bsize,
+                           double4 *partial, double *out_dev, int *err, cudaStream_t s) {
+  norms_partial_kernel<A, Rt><<<nlist, 256, 0, s>>>(
+      reinterpret_cast<const A *>(a->dat) + a->offset, a->step, reinterpret_cast<const Rt *>(r->dat) + r->offset,
+      r->step, blist, nlist, bsize, a->chunks, r->chunks, partial, err);
+  norms_final_kernel<<<1, 256, 0, s>>>(partial, (int)nlist, out_dev);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "no-alloc norm kernels launch");
+  return BK_OK;
+}
+
+}  // namespace bk
+
+extern "C" int bk_field_norms_noalloc(const bk_field *a, const bk_field *ref, const unsigned *blist, unsigned nlist,
+                                      const bk_layout *lay, void *stream, double out[4]) {
+  using namespace bk;
+  Layout L;
+  int s = check_pair(a, ref, lay, blist, nlist, &L);
+  if (s) return s;
+  if (!out) return fail(BK_ERR_ARG, "out is NULL");
+  if (nlist > (unsigned)NOALLOC_MAX_BRICKS)
+    return fail(BK_ERR_ARG, "bk_field_norms_noalloc: " + std::to_string(nlist) +
+                                " bricks exceed its static scratch of " + std::to_string(NOALLOC_MAX_BRICKS) +
+                                " bricks; split the list and combine (max of maxima, sum of sums)");
+  for (int q = 0; q < 4; ++q) out[q] = 0.0;
+  if (nlist == 0) return BK_OK;
+  double4 *scratch = nullptr;
+  if ((s = noalloc_scratch(&scratch))) return s;
+  double4 *partial = scratch;
+  double *res = reinterpret_cast<double *>(scratch + NOALLOC_MAX_BRICKS);
+  int *err = reinterpret_cast<int *>(scratch + NOALLOC_MAX_BRICKS + 1);
+  cudaStream_t st = as_stream(stream);
+  BK_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));  // the word starts each call at zero
+#define BK_NORM_CASE(DA, TA, DR, TR)                                                                  \
+  if (a->dtype == DA && ref->dtype == DR) {                                                           \
+    s = launch_norms_per_brick<TA, TR>(a, ref, blist, nlist, L.size(), partial, res, err, st);       \
+  } else
+  BK_NORM_CASE(BK_F64, double, BK_F64, double)
+  BK_NORM_CASE(BK_F32, float, BK_F64, double)
+  BK_NORM_CASE(BK_BF16, __nv_bfloat16, BK_F64, double)
+  BK_NORM_CASE(BK_F32, float, BK_F32, float)
+  BK_NORM_CASE(BK_BF16, __nv_bfloat16, BK_BF16, __nv_bfloat16)
+  BK_NORM_CASE(BK_F64, double, BK_F32, float)
+  BK_NORM_CASE(BK_F64, double, BK_BF16, __nv_bfloat16)
+  BK_NORM_CASE(BK_F32, float, BK_BF16, __nv_bfloat16)
+  BK_NORM_CASE(BK_BF16, __nv_bfloat16, BK_F32, float)
+  return fail(BK_ERR_ARG, "unknown dtype pair");
+#undef BK_NORM_CASE
+  if (s) return s;
+  int herr = 0;
+  BK_CUDA(cudaMemcpyAsync(out, res, sizeof(double) * 4, cudaMemcpyDeviceToHost, st));
+  BK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BK_CUDA(cudaStreamSynchronize(st));
+  if (herr) return fail(BK_ERR_BOUNDS, "bk_field_norms_noalloc: a listed brick index was out of range and skipped");
+  return BK_OK;
+}

@@ -189,6 +189,23 @@ int bk_convert(const bk_field *src, const bk_field *dst, const unsigned *blist, 
 int bk_field_norms(const bk_field *a, const bk_field *ref, const unsigned *blist, unsigned nlist,
                    const bk_layout *lay, void *stream, double out[4]);
 
+/* bk_field_norms without any allocation, for callers that cannot call cudaMalloc: a
+ * serving loop with a latency budget (cudaMalloc / cudaFree can synchronise the device and
+ * stall every stream) or a process whose device memory is all reserved up front by another
+ * allocator.  No counterpart in the reference.
+ * Same inputs and outputs as bk_field_norms; its scratch (one FP64 partial per listed brick,
+ * the result and an error word, ~512 KiB) is a file-scope static device array that every GPU
+ * loading this library holds until exit, so nlist may not exceed
+ * BK_NORMS_NOALLOC_MAX_BRICKS (larger lists: split them and combine -- max of the maxima,
+ * sum of the sums).  Calls no cudaMalloc / cudaFree.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) for that device; make that first call
+ * before any stream capture.  All calls share the array and it keeps the last call's
+ * contents: calls whose work overlaps on the GPU race.  Synchronises the stream; returns
+ * BK_ERR_BOUNDS when a listed brick was out of range. */
+#define BK_NORMS_NOALLOC_MAX_BRICKS 16384
+int bk_field_norms_noalloc(const bk_field *a, const bk_field *ref, const unsigned *blist, unsigned nlist,
+                           const bk_layout *lay, void *stream, double out[4]);
+
 /* Seeded initial field: the sum of `nwaves` sines with integer wave numbers in 1..4 and
  * random phases on the periodic interior, plus `noise` times uniform[-1,1) noise, written
  * to every brick of an init_grid layout of grid_bricks (k,j,i) bricks with ghost_bricks
