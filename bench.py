@@ -48,7 +48,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-alt", action="store_true")
-    p.add_argument("--form", default="plain", choices=["plain", "precision"],
+    p.add_argument("--ndom", type=int, default=256)
+    p.add_argument("--form", default="plain", choices=["plain", "precision", "batched"],
                    help="plain: the FP64 drop-in bench line; precision: the precision-form error study")
     return p.parse_args()
 
@@ -413,11 +414,88 @@ def run_precision(args):
                           "reference": "FP64 native run on the device", "records": recs}), flush=True)
 
 
+def run_batched(args):
+    """The batched form (BASELINE config 4): autotune the layout, then 10 FP32 steps of all 256
+    domains from one captured graph, against the plain FP64 drop-in run domain by domain (and
+    an unbatched FP32 run), with the FP32 error against FP64."""
+    import torch
+    from bricklib_gb300 import _abi, batch as BT, bricks as B
+    from bricklib_gb300._abi import call
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    call("bk_set_device", local)
+    stream = torch.cuda.current_stream()
+    w = BT.make_workload(ndom=args.ndom)
+    steps = 10
+    t0 = time.perf_counter()
+    tune = BT.autotune(w, _abi.BK_F32, _abi.BK_ACC_NATIVE, steps=steps, use_cache=False)
+    tune_s = time.perf_counter() - t0
+    best = tune["best"]
+    lay = B.Layout(tuple(best["bdim"]), tuple(best["fold"]))
+    bt = BT.Batch(w, lay, _abi.BK_F32)
+    call("bk_batch_set_grid", bt.h, best["grid_cap"])
+    t_batch = BT.time_batch(bt, steps, reps=5)
+    gst_batch = w.points * steps / t_batch / 1e9
+
+    def unbatched(dtype, lay_):
+        tot = 0.0
+        outs = []
+        for spec in w.domains:
+            ds = BT.DomainStorage(spec, lay_, dtype)
+            BT.init_domain(ds, stream.cuda_stream)
+            plan, lst = B.GhostPlan(ds.pairs), B.BrickList(ds.interior)
+            st = B.to_c_stencil(w.stencils[spec.stencil])
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            B.timeSteps(ds.field(0), ds.field(1), lst, st, steps, plan=plan, stream=stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1) * 1e-3
+            outs.append((ds, lst))
+        return tot, outs
+
+    t_plain64, outs64 = unbatched(_abi.BK_F64, B.DEFAULT_LAYOUT)
+    t_plain32, _ = unbatched(_abi.BK_F32, B.DEFAULT_LAYOUT)
+    # error of the batched FP32 result against the plain FP64 result, domain by domain
+    # (compare on the FP64 run's layout when the batch chose another one)
+    worst = 0.0
+    if lay == B.DEFAULT_LAYOUT:
+        for (ds64, lst), ds32 in zip(outs64, bt.doms):
+            nrm = B.fieldNorms(ds32.field(bt.parity), ds64.field(steps % 2), lst)
+            worst = max(worst, nrm["max_rel"])
+    else:
+        b8 = BT.Batch(w, B.DEFAULT_LAYOUT, _abi.BK_F32)
+        b8.run(steps, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        for (ds64, lst), ds32 in zip(outs64, b8.doms):
+            nrm = B.fieldNorms(ds32.field(b8.parity), ds64.field(steps % 2), lst)
+            worst = max(worst, nrm["max_rel"])
+        b8.close()
+    if rank == 0:
+        print(json.dumps({
+            "form": "batched", "metric": "GStencil/s", "unit": "GStencil/s",
+            "domains": len(w.domains), "interior_points": w.points, "steps": steps,
+            "batched_fp32": {"value": round(gst_batch, 2), "ms_per_10_steps": round(t_batch * 1e3, 3),
+                             "layout": {"bdim": lay.bdim, "fold": lay.fold, "grid_cap": best["grid_cap"]},
+                             "graph": True, "launches_per_step": 2},
+            "plain_fp64_per_domain": {"value": round(w.points * steps / t_plain64 / 1e9, 2),
+                                      "ms": round(t_plain64 * 1e3, 2)},
+            "unbatched_fp32_per_domain": {"value": round(w.points * steps / t_plain32 / 1e9, 2),
+                                          "ms": round(t_plain32 * 1e3, 2)},
+            "batched_vs_plain": round(t_plain64 / t_batch, 2),
+            "fp32_max_normwise_err_vs_fp64": worst,
+            "autotune": {"seconds": round(tune_s, 1), "table": tune["table"]}}), flush=True)
+    bt.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.form == "precision":
         run_precision(a)
+    elif a.form == "batched":
+        run_batched(a)
     else:
         run_ours(a)

@@ -42,6 +42,12 @@ class bk_stencil(C.Structure):
                 ("coeff", C.c_double * BK_MAX_TAPS)]
 
 
+class bk_batch_domain(C.Structure):
+    _fields_ = [("adj", C.c_void_p), ("nbricks", C.c_uint), ("dat", C.c_void_p), ("chunks", C.c_long),
+                ("step", C.c_size_t), ("off0", C.c_size_t), ("off1", C.c_size_t), ("blist", C.c_void_p),
+                ("nlist", C.c_uint), ("pairs", C.c_void_p), ("npairs", C.c_uint), ("stencil", C.c_int)]
+
+
 _vp = C.c_void_p
 _P = C.POINTER
 
@@ -77,6 +83,12 @@ SIGNATURES = {
                                          _P(C.c_double)]),
     "bk_fill_sines": (C.c_int, [_P(bk_field), _P(bk_layout), _P(C.c_long), _P(C.c_long), C.c_int, C.c_uint64,
                                 C.c_double, _vp]),
+    "bk_batch_create": (C.c_int, [_P(_vp), _P(bk_batch_domain), C.c_uint, _P(bk_stencil), C.c_uint,
+                                  _P(bk_layout), C.c_int, C.c_int]),
+    "bk_batch_set_grid": (C.c_int, [_vp, C.c_int]),
+    "bk_batch_run": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "bk_batch_parity": (C.c_int, [_vp]),
+    "bk_batch_destroy": (C.c_int, [_vp]),
     "bk_steps": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_field), _vp, C.c_uint, _vp, C.c_uint,
                            _P(bk_stencil), _P(bk_layout), C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
 }

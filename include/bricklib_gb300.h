@@ -226,6 +226,49 @@ int bk_steps(const unsigned *adj, unsigned nbricks, const bk_field *a, const bk_
              const bk_stencil *st, const bk_layout *lay, int acc, int steps, int fill_every,
              int use_graph, void *stream);
 
+/* ------------------------------------------------------------------ batched form */
+
+/* One domain of a batch: an independent brick grid with two ping-pong fields in one
+ * device storage, the bricks to compute each step and its ghost plan (host arrays, copied
+ * at creation).  The reference advances several subdomains in one launch in
+ * strong/main.cu:85-100 (brick_kernel over Brick3D barr[], subdomain = blockIdx.x / strideb);
+ * a batch generalises that to domains of any size and stencil. */
+typedef struct bk_batch_domain {
+  const unsigned *adj;   /* device adjacency, nbricks x 27 */
+  unsigned nbricks;
+  void *dat;             /* device storage holding both fields */
+  long chunks;
+  size_t step;           /* elements per chunk */
+  size_t off0, off1;     /* element offsets of the two ping-pong fields */
+  const unsigned *blist; /* host: bricks computed every step */
+  unsigned nlist;
+  const unsigned *pairs; /* host: ghost plan, npairs (dst, src) brick pairs */
+  unsigned npairs;
+  int stencil;           /* index into the batch's stencil array */
+} bk_batch_domain;
+
+typedef struct bk_batch bk_batch;
+
+/* Build a batch: domains share one layout, one storage type and one accumulation mode;
+ * stencils are 7/13-point stars and 27/125-point cubes (radius 1 or 2, up to 8 of them).
+ * Builds the global (domain, brick) work list and (domain, dst, src) fill list on the
+ * device.  Field 0 (off0) holds the input of the first step. */
+int bk_batch_create(bk_batch **batch, const bk_batch_domain *doms, unsigned ndom, const bk_stencil *stencils,
+                    unsigned nstencils, const bk_layout *lay, int dtype, int acc);
+/* Cap the number of CTAs of the persistent sweep launch (0 = one CTA per work group);
+ * the autotuner's block-count knob. */
+int bk_batch_set_grid(bk_batch *batch, int max_ctas);
+/* Advance every domain `steps` steps: before every `fill_every`-th step (0 = never) the ghost
+ * plans are applied to the current input fields, then one persistent launch sweeps the whole
+ * work list.  With use_graph the sequence is captured once per (steps, fill_every, parity)
+ * into a CUDA graph kept by the batch and replayed on later calls. */
+int bk_batch_run(bk_batch *batch, int steps, int fill_every, int use_graph, void *stream);
+/* Which field (0 or 1) holds the newest values. */
+int bk_batch_parity(const bk_batch *batch);
+/* Synchronises the device and releases the batch's device memory and graphs; the domains'
+ * storages belong to the caller. */
+int bk_batch_destroy(bk_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,143 @@
+"""Batched form: many uneven periodic domains in one persistent launch per step."""
+import numpy as np
+import pytest
+
+from bricklib_gb300 import batch as BT, bricks as B, stencils
+from bricklib_gb300._abi import BK_ACC_COMPENSATED, BK_ACC_NATIVE, BK_F32, BK_F64
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def small_workload(nd=8, multiple=8, hi=48):
+    return BT.make_workload(ndom=nd, seed=9, lo=16, hi=hi, multiple=multiple)
+
+
+def fields(b, which):
+    out = []
+    for ds in b.doms:
+        host = B.movBrickStorage(ds.storage, to_device=False).host
+        out.append(host.reshape(ds.nbricks, -1)[:, which * ds.lay.size:(which + 1) * ds.lay.size].copy())
+    return out
+
+
+def per_domain_steps(w, lay, dtype, steps, acc=BK_ACC_NATIVE):
+    res = []
+    for spec in w.domains:
+        ds = BT.DomainStorage(spec, lay, dtype)
+        BT.init_domain(ds)
+        plan = B.GhostPlan(ds.pairs)
+        lst = B.BrickList(ds.interior)
+        B.timeSteps(ds.field(0), ds.field(1), lst, w.stencils[spec.stencil], steps, plan=plan, acc=acc,
+                    use_graph=False)
+        B.synchronize()
+        host = B.movBrickStorage(ds.storage, to_device=False).host
+        res.append(host.reshape(ds.nbricks, -1)[:, (steps % 2) * lay.size:((steps % 2) + 1) * lay.size].copy())
+    return res
+
+
+def test_batch_equals_per_domain_runs_and_oracle():
+    w = small_workload()
+    lay = B.Layout()
+    steps = 6
+    b = BT.Batch(w, lay, BK_F32)
+    b.run(steps, use_graph=True)
+    B.synchronize()
+    assert b.parity == steps % 2
+    got = fields(b, b.parity)
+    want = per_domain_steps(w, lay, BK_F32, steps)
+    ref64 = per_domain_steps(w, lay, BK_F64, steps)
+    for d, spec in enumerate(w.domains):
+        ds = b.doms[d]
+        idx = ds.interior
+        g, f32, f64 = got[d][idx], want[d][idx], ref64[d][idx]
+        # same storage type, per-domain launch vs batch: FP32 arithmetic up to tap grouping
+        assert np.abs(g - f32).max() <= 1e-6 * np.abs(f64).max(), d
+        # the FP32 batch against the FP64 run of the same domain: the 1e-5 spec
+        assert np.abs(g - f64).max() <= 1e-5 * np.abs(f64).max(), d
+    # one domain against the CPU oracle (FP64 array path from the same initial values)
+    spec = w.domains[0]
+    ds = BT.DomainStorage(spec, lay, BK_F64)
+    BT.init_domain(ds)
+    host0 = B.movBrickStorage(ds.storage, to_device=False).host
+    n = spec.n
+    odom = oracle.Domain(n)
+    a = odom.from_bricks(host0, 0)
+    # from_bricks copies only the interior: refill the ghost zone periodically each step
+    o = odom.ghost + odom.pad
+    st = w.stencils[spec.stencil]
+    bb = np.zeros_like(a)
+    for _ in range(steps):
+        oracle.array_periodic_fill(a, (o,) * 3, n, (8, 8, 8))
+        oracle.array_sweep(a, bb, (o,) * 3, tuple(o + x for x in n), st.offsets(), st.coeff)
+        a, bb = bb, a
+    dat = odom.alloc()
+    odom.to_bricks(a, dat, 0)
+    orc = dat.reshape(odom.nbricks, odom.step)[:, :odom.bsize][ds.interior]
+    assert np.abs(got[0][ds.interior] - orc).max() <= 1e-5 * np.abs(orc).max()
+    b.close()
+
+
+def test_batch_graph_and_plain_bitwise_equal_and_layouts_agree():
+    w = small_workload(nd=6, multiple=32, hi=64)
+    res = []
+    for g in (True, False):
+        b = BT.Batch(w, B.Layout(), BK_F32)
+        b.run(4, use_graph=g)
+        B.synchronize()
+        res.append(fields(b, b.parity))
+        b.close()
+    for x, y in zip(*res):
+        np.testing.assert_array_equal(x, y)
+    # the point arithmetic does not depend on the brick layout: compare interiors as arrays
+    base = None
+    for bdim, fold in BT.CANDIDATES:
+        lay = B.Layout(bdim, fold)
+        assert BT.layout_valid(w, lay)
+        b = BT.Batch(w, lay, BK_F32)
+        b.run(4)
+        B.synchronize()
+        arrs = []
+        for ds, f in zip(b.doms, fields(b, b.parity)):
+            dat = np.zeros(ds.nbricks * 2 * lay.size, np.float32)
+            dat.reshape(ds.nbricks, -1)[:, :lay.size] = f
+            st = B.BrickStorage(ds.nbricks, 2 * lay.size, BK_F32, host=dat)
+            arr = np.zeros(tuple(x + 2 * b_ + 16 for x, b_ in zip(ds.spec.n, bdim)))
+            B.copyFromBrick(list(reversed(ds.spec.n)), [8] * 3, list(reversed(bdim)), arr, ds.grid,
+                            B.Brick(ds.info, st, 0, lay))
+            arrs.append(arr[tuple(slice(8 + b_, 8 + b_ + x) for x, b_ in zip(ds.spec.n, bdim))])
+        b.close()
+        if base is None:
+            base = arrs
+        else:
+            for x, y in zip(base, arrs):
+                np.testing.assert_array_equal(x, y)
+
+
+def test_domain_alone_equals_domain_in_the_mix():
+    w = small_workload(nd=5)
+    b = BT.Batch(w, B.Layout(), BK_F32, BK_ACC_COMPENSATED)
+    b.run(3)
+    B.synchronize()
+    mix = fields(b, b.parity)
+    b.close()
+    for d in (0, 3):
+        alone = BT.Workload([w.domains[d]], w.stencils)
+        b1 = BT.Batch(alone, B.Layout(), BK_F32, BK_ACC_COMPENSATED)
+        b1.run(3)
+        B.synchronize()
+        np.testing.assert_array_equal(fields(b1, b1.parity)[0], mix[d])
+        b1.close()
+
+
+def test_batch_rejects_bad_domains():
+    from bricklib_gb300 import _abi
+    import ctypes as C
+    w = small_workload(nd=1)
+    ds = BT.DomainStorage(w.domains[0], B.Layout(), BK_F32)
+    d = ds.desc(5)  # stencil index out of range
+    sts = (_abi.bk_stencil * 1)(B.to_c_stencil(w.stencils[0]))
+    h = C.c_void_p()
+    st = _abi.lib().bk_batch_create(C.byref(h), C.byref(d), 1, sts, 1, C.byref(B.Layout().to_c()), BK_F32, 0)
+    assert st == _abi.BK_ERR_ARG
+    assert b"malformed" in _abi.lib().bk_last_error()
