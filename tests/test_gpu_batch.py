@@ -89,12 +89,24 @@ def test_batch_graph_and_plain_bitwise_equal_and_layouts_agree():
         b.close()
     for x, y in zip(*res):
         np.testing.assert_array_equal(x, y)
-    # the point arithmetic does not depend on the brick layout: compare interiors as arrays
+    # the point arithmetic does not depend on the brick layout: load the same arrays into
+    # every layout (copyToBrick), run, and compare the interiors as arrays
+    arrays = []
+    for spec in w.domains:
+        arrays.append(stencils.uniform(spec.seed, int(np.prod([x + 2 * 32 + 16 for x in spec.n]))))
     base = None
     for bdim, fold in BT.CANDIDATES:
         lay = B.Layout(bdim, fold)
         assert BT.layout_valid(w, lay)
-        b = BT.Batch(w, lay, BK_F32)
+        b = BT.Batch(w, lay, BK_F32, init=False)
+        for ds, a in zip(b.doms, arrays):
+            big = a.reshape([x + 2 * 32 + 16 for x in ds.spec.n])
+            sub = big[tuple(slice(32 - b_, 32 - b_ + x + 2 * b_ + 16) for x, b_ in zip(ds.spec.n, bdim))]
+            host = np.zeros(ds.nbricks * 2 * lay.size, np.float32)
+            st = B.BrickStorage(ds.nbricks, 2 * lay.size, BK_F32, host=host)
+            g = [x + 2 * b_ for x, b_ in zip(reversed(ds.spec.n), reversed(bdim))]
+            B.copyToBrick(g, [8] * 3, [0] * 3, np.ascontiguousarray(sub), ds.grid, B.Brick(ds.info, st, 0, lay))
+            ds.storage.device.upload(host)
         b.run(4)
         B.synchronize()
         arrs = []
