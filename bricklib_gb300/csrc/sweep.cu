@@ -157,6 +157,20 @@ static Taps &thread_taps() {
   return t;
 }
 
+// Stencil analysis and accumulation mode for kernels outside this file (the batch).
+int plan_stencil(const bk_stencil *st, const Layout &L, int dtype, int acc, SweepPlan *plan, Taps *tp) {
+  int s = analyze(st, L, plan, tp);
+  if (s) return s;
+  if (plan->shape < 0) return fail(BK_ERR_UNSUPPORTED, "brick dims must be 8x8x8, 4x4x4, 16x8x8 or 8x8x32");
+  plan->dtype = dtype;
+  plan->v2 = false;
+  if (acc == BK_ACC_NATIVE) plan->acc = ACCM_NATIVE;
+  else if (acc == BK_ACC_COMPENSATED && dtype != BK_F64) plan->acc = ACCM_COMP;
+  else if (acc == BK_ACC_FLOATFLOAT && dtype == BK_F64) plan->acc = ACCM_FF;
+  else return fail(BK_ERR_UNSUPPORTED, "accumulation mode not available for this storage type");
+  return BK_OK;
+}
+
 }  // namespace bk
 
 using namespace bk;

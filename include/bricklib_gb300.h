@@ -249,10 +249,10 @@ typedef struct bk_batch_domain {
 
 typedef struct bk_batch bk_batch;
 
-/* Build a batch: domains share one layout, one storage type and one accumulation mode;
- * stencils are 7/13-point stars and 27/125-point cubes (radius 1 or 2, up to 8 of them).
- * Builds the global (domain, brick) work list and (domain, dst, src) fill list on the
- * device.  Field 0 (off0) holds the input of the first step. */
+/* Build a batch: domains share one layout, one storage type (FP64 or FP32) and one
+ * accumulation mode; up to 8 stencils, any that bk_sweep accepts.  Builds on the device the
+ * global (domain, brick) work list, sorted by stencil, and the (domain, dst, src) fill list.
+ * Field 0 (off0) holds the input of the first step. */
 int bk_batch_create(bk_batch **batch, const bk_batch_domain *doms, unsigned ndom, const bk_stencil *stencils,
                     unsigned nstencils, const bk_layout *lay, int dtype, int acc);
 /* Cap the number of CTAs of the persistent sweep launch (0 = one CTA per work group);
