@@ -89,6 +89,10 @@ SIGNATURES = {
     "bk_batch_run": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp]),
     "bk_batch_parity": (C.c_int, [_vp]),
     "bk_batch_destroy": (C.c_int, [_vp]),
+    "bk_copy_to_bricks": (C.c_int, [_vp, _P(C.c_long), _P(C.c_long), _P(C.c_long), _vp, _P(bk_field),
+                                    _P(bk_layout), _vp]),
+    "bk_copy_from_bricks": (C.c_int, [_vp, _P(C.c_long), _P(C.c_long), _P(C.c_long), _vp, _P(bk_field),
+                                      _P(bk_layout), _vp]),
     "bk_steps": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_field), _vp, C.c_uint, _vp, C.c_uint,
                            _P(bk_stencil), _P(bk_layout), C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
 }

@@ -486,3 +486,22 @@ def fillSines(brick: Brick, grid_bricks, ghost_bricks, nwaves: int = 8, seed: in
     """The seeded sum-of-sines initial field on every brick of an init_grid layout."""
     call("bk_fill_sines", C.byref(brick.field()), C.byref(brick.layout.to_c()), (C.c_long * 3)(*grid_bricks),
          (C.c_long * 3)(*ghost_bricks), nwaves, seed, noise, stream_ptr(stream))
+
+
+# ------------------------------------------------------------------ array <-> bricks on the device
+
+def copyToBrickDevice(dimlist, padding, ghost, arr_dev: int, grid_dev: int, brick: Brick, stream=None) -> None:
+    """copyToBrick with the array and grid on the device (bk_copy_to_bricks); lists are
+    contiguous-first like the host copyToBrick."""
+    L3 = C.c_long * 3
+    call("bk_copy_to_bricks", C.c_void_p(arr_dev), L3(*reversed(dimlist)), L3(*reversed(padding)),
+         L3(*reversed(ghost)), C.c_void_p(grid_dev), C.byref(brick.field()), C.byref(brick.layout.to_c()),
+         stream_ptr(stream))
+
+
+def copyFromBrickDevice(dimlist, padding, ghost, arr_dev: int, grid_dev: int, brick: Brick, stream=None) -> None:
+    """copyFromBrick on the device (bk_copy_from_bricks)."""
+    L3 = C.c_long * 3
+    call("bk_copy_from_bricks", C.c_void_p(arr_dev), L3(*reversed(dimlist)), L3(*reversed(padding)),
+         L3(*reversed(ghost)), C.c_void_p(grid_dev), C.byref(brick.field()), C.byref(brick.layout.to_c()),
+         stream_ptr(stream))

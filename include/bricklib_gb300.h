@@ -214,6 +214,20 @@ int bk_field_norms_noalloc(const bk_field *a, const bk_field *ref, const unsigne
 int bk_fill_sines(const bk_field *f, const bk_layout *lay, const long grid_bricks[3],
                   const long ghost_bricks[3], int nwaves, uint64_t seed, double noise, void *stream);
 
+/* ------------------------------------------------------------------ array <-> bricks */
+
+/* copyToBrick / copyFromBrick (include/bricksetup.h:172-221) on the device: the region
+ * dim (k,j,i) of a device array of extent dim + 2*(pad + ghost) is copied to / from the
+ * bricks at grid positions ghost/B .. (dim+ghost)/B - 1, grid (device, row-major over
+ * (dim + 2*ghost)/B bricks per axis) mapping positions to storage indices, as the host
+ * copies do with grid_ptr.  The array has the field's element type.  pad may be negative
+ * down to -ghost (an array holding the region without its ghost cells).  The reference
+ * times these host copies as "To"/"From" in stencils/copy.cpp:32-58. */
+int bk_copy_to_bricks(const void *arr, const long dim[3], const long pad[3], const long ghost[3],
+                      const unsigned *grid, const bk_field *f, const bk_layout *lay, void *stream);
+int bk_copy_from_bricks(void *arr, const long dim[3], const long pad[3], const long ghost[3],
+                        const unsigned *grid, const bk_field *f, const bk_layout *lay, void *stream);
+
 /* ------------------------------------------------------------------ time steps */
 
 /* T time steps, ping-pong between fields a and b (weak/main.cu:277-282): before every
