@@ -49,7 +49,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-alt", action="store_true")
     p.add_argument("--ndom", type=int, default=256)
-    p.add_argument("--form", default="plain", choices=["plain", "precision", "batched"],
+    p.add_argument("--rates", default="200,2000")
+    p.add_argument("--njobs", type=int, default=400)
+    p.add_argument("--form", default="plain", choices=["plain", "precision", "batched", "serving"],
                    help="plain: the FP64 drop-in bench line; precision: the precision-form error study")
     return p.parse_args()
 
@@ -485,6 +487,27 @@ def run_batched(args):
     bt.close()
 
 
+def run_serving(args):
+    """The serving form (BASELINE config 5): Poisson arrivals of the mixed job set at each rate
+    against the continuous-batching server; p50 / p99 latency and aggregate GStencil/s."""
+    import torch
+    from bricklib_gb300 import _abi, serving
+    from bricklib_gb300._abi import call
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    call("bk_set_device", local)
+    res = []
+    for rate in [float(r) for r in args.rates.split(",")]:
+        for acc_name, acc in (("native", _abi.BK_ACC_NATIVE), ("floatfloat", _abi.BK_ACC_FLOATFLOAT)):
+            st = serving.run_load(rate, args.njobs, fp64_acc=acc)
+            st["fp64_arithmetic"] = acc_name
+            res.append(st)
+    if rank == 0:
+        print(json.dumps({"form": "serving", "metric": "p50/p99 latency (s), GStencil/s", "budget_bytes": 150e9,
+                          "jobs": "edges log-uniform [16,192] (multiples of 8), 5 shapes, steps U[1,200], "
+                                  "50% FP64 / 50% FP32", "runs": res}), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -493,5 +516,7 @@ if __name__ == "__main__":
         run_precision(a)
     elif a.form == "batched":
         run_batched(a)
+    elif a.form == "serving":
+        run_serving(a)
     else:
         run_ours(a)

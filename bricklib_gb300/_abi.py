@@ -48,6 +48,18 @@ class bk_batch_domain(C.Structure):
                 ("nlist", C.c_uint), ("pairs", C.c_void_p), ("npairs", C.c_uint), ("stencil", C.c_int)]
 
 
+class bk_job_desc(C.Structure):
+    _fields_ = [("n", C.c_long * 3), ("stencil", C.POINTER(bk_stencil)), ("steps", C.c_int), ("dtype", C.c_int),
+                ("acc", C.c_int), ("input", C.c_void_p), ("output", C.c_void_p)]
+
+
+class bk_server_report(C.Structure):
+    _fields_ = [("submitted", C.c_ulonglong), ("admitted", C.c_ulonglong), ("completed", C.c_ulonglong),
+                ("rejected", C.c_ulonglong), ("ticks", C.c_ulonglong), ("p50_s", C.c_double), ("p99_s", C.c_double),
+                ("mean_s", C.c_double), ("max_s", C.c_double), ("gstencil_s", C.c_double), ("span_s", C.c_double),
+                ("hbm_budget", C.c_size_t), ("hbm_peak", C.c_size_t)]
+
+
 _vp = C.c_void_p
 _P = C.POINTER
 
@@ -93,6 +105,12 @@ SIGNATURES = {
                                     _P(bk_layout), _vp]),
     "bk_copy_from_bricks": (C.c_int, [_vp, _P(C.c_long), _P(C.c_long), _P(C.c_long), _vp, _P(bk_field),
                                       _P(bk_layout), _vp]),
+    "bk_server_create": (C.c_int, [_P(_vp), C.c_size_t, _P(bk_layout), C.c_int]),
+    "bk_server_submit": (C.c_int, [_vp, _P(bk_job_desc), _P(C.c_ulonglong)]),
+    "bk_server_wait": (C.c_int, [_vp, C.c_ulonglong, C.c_double, _P(C.c_double)]),
+    "bk_server_drain": (C.c_int, [_vp, C.c_double]),
+    "bk_server_stats": (C.c_int, [_vp, _P(bk_server_report)]),
+    "bk_server_destroy": (C.c_int, [_vp]),
     "bk_steps": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_field), _vp, C.c_uint, _vp, C.c_uint,
                            _P(bk_stencil), _P(bk_layout), C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
 }

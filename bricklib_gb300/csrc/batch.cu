@@ -13,20 +13,9 @@
 #include <utility>
 #include <vector>
 
-#include "sweep_kernel.cuh"
+#include "batch_common.cuh"
 
 namespace bk {
-
-constexpr int BATCH_MAX_ST = 8;
-
-struct BatchDomain {  // device table entry
-  const unsigned *adj;
-  unsigned nbricks;
-  unsigned stencil;
-  unsigned char *f0, *f1;  // field bases (dat + offset), bytes
-  unsigned long long step_bytes;
-  long long chunks;
-};
 
 // Per-stencil sweep over a segment of the global work list: the one-shot brick kernel
 // (sweep_kernel) with every slot resolving its own domain -- adjacency, ping-pong fields and
@@ -155,12 +144,6 @@ int launch_batch_sweep(const BatchDomain *doms, unsigned ndom, const uint2 *work
   return BK_OK;
 }
 
-// What one per-stencil launch needs besides the work segment.
-struct BatchStencil {
-  SweepPlan plan;  // family, radius, accumulation, shape, row-major
-  Taps taps;
-};
-
 template <typename T, int ACC>
 int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndom, const uint2 *work, unsigned nwork,
                    int parity, const Layout &L, int *err, int grid_cap, cudaStream_t s) {
@@ -211,6 +194,34 @@ struct bk_batch {
 namespace bk {
 
 int plan_stencil(const bk_stencil *st, const Layout &L, int dtype, int acc, SweepPlan *plan, Taps *tp);
+
+// Launchers shared with the server (serve.cu): one stencil over a work segment, and the
+// batched ghost fill.
+int batch_launch_sweep(const BatchStencil &bs, int dtype, const BatchDomain *doms, unsigned ndom, const uint2 *work,
+                       unsigned nwork, int parity, const Layout &L, int *err, int grid_cap, cudaStream_t s) {
+  if (!nwork) return BK_OK;
+  const int acc = bs.plan.acc;
+  if (dtype == BK_F32)
+    return acc == ACCM_COMP ? batch_dispatch<float, ACCM_COMP>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s)
+                            : batch_dispatch<float, ACCM_NATIVE>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s);
+  if (dtype == BK_F64)
+    return acc == ACCM_FF ? batch_dispatch<double, ACCM_FF>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s)
+                          : batch_dispatch<double, ACCM_NATIVE>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s);
+  return fail(BK_ERR_UNSUPPORTED, "batch: BF16 storage is not instantiated");
+}
+
+int batch_launch_fill(const BatchDomain *doms, unsigned ndom, const uint3 *pairs, unsigned npairs, int parity,
+                      size_t brick_bytes, int *err, cudaStream_t s) {
+  if (!npairs) return BK_OK;
+  const unsigned grid = npairs < (1u << 30) ? npairs : (1u << 30);
+  if (brick_bytes % 16 == 0)
+    batch_fill_kernel<uint4><<<grid, 256, 0, s>>>(doms, ndom, pairs, npairs, parity, (unsigned)(brick_bytes / 16), err);
+  else
+    batch_fill_kernel<unsigned short><<<grid, 256, 0, s>>>(doms, ndom, pairs, npairs, parity, (unsigned)(brick_bytes / 2), err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "batch fill launch");
+  return BK_OK;
+}
 
 static int batch_sweep(bk_batch *b, cudaStream_t s) {
   for (size_t q = 0; q < b->sts.size(); ++q) {

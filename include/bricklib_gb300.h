@@ -283,6 +283,49 @@ int bk_batch_parity(const bk_batch *batch);
  * storages belong to the caller. */
 int bk_batch_destroy(bk_batch *batch);
 
+/* ------------------------------------------------------------------ serving form */
+
+/* One stencil job: a periodic domain of n (k,j,i) interior cells (multiples of the server's
+ * brick dims), advanced `steps` steps with `stencil` in storage type dtype (BK_F64 or
+ * BK_F32) and accumulation acc.  input / output are host arrays of n[0]*n[1]*n[2] elements
+ * (k, j, i; i contiguous) that must stay valid until the job completes; page-locked memory
+ * (bk_host_malloc) lets their copies overlap with other jobs' work. */
+typedef struct bk_job_desc {
+  long n[3];
+  const bk_stencil *stencil;
+  int steps;
+  int dtype;
+  int acc;
+  const void *input;
+  void *output;
+} bk_job_desc;
+
+typedef struct bk_server_report {
+  unsigned long long submitted, admitted, completed, rejected, ticks;
+  double p50_s, p99_s, mean_s, max_s; /* latency: submission to output on the host */
+  double gstencil_s;                  /* completed point-steps / (last completion - first submission) */
+  double span_s;
+  size_t hbm_budget, hbm_peak;        /* bytes admitted against the budget: limit and peak */
+} bk_server_report;
+
+typedef struct bk_server bk_server;
+
+/* Start a server on the current device: jobs are admitted first-in first-out while their
+ * device bytes (storage, adjacency, staging, work lists) fit in hbm_budget and fewer than
+ * max_active jobs run.  Every active job advances one step per scheduler tick; jobs join
+ * and leave between ticks.  Layout: a row-major brick layout (e.g. 8x8x8, fold (4,8)). */
+int bk_server_create(bk_server **server, size_t hbm_budget, const bk_layout *lay, int max_active);
+/* Queue a job (thread safe).  BK_ERR_BUDGET when the job alone exceeds the budget. */
+int bk_server_submit(bk_server *server, const bk_job_desc *job, unsigned long long *id);
+/* Wait up to timeout_s for a job; BK_ERR_TIMEOUT if it is not done by then.  On success
+ * the output array holds the result and *latency_s the submission-to-result time. */
+int bk_server_wait(bk_server *server, unsigned long long id, double timeout_s, double *latency_s);
+/* Wait up to timeout_s for every submitted job. */
+int bk_server_drain(bk_server *server, double timeout_s);
+int bk_server_stats(bk_server *server, bk_server_report *stats);
+/* Stop the scheduler (jobs not yet done are abandoned), free all device memory. */
+int bk_server_destroy(bk_server *server);
+
 #ifdef __cplusplus
 }
 #endif
