@@ -39,7 +39,10 @@ class bk_field(C.Structure):
 
 class bk_stencil(C.Structure):
     _fields_ = [("npoints", C.c_int), ("offsets", (C.c_int * 3) * BK_MAX_TAPS),
-                ("coeff", C.c_double * BK_MAX_TAPS)]
+                ("coeff", C.c_double * BK_MAX_TAPS), ("pre_op", C.c_int), ("post_op", C.c_int)]
+
+
+BK_OP_NONE, BK_OP_RELU, BK_OP_ABS = 0, 1, 2
 
 
 class bk_batch_domain(C.Structure):

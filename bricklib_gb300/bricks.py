@@ -380,6 +380,7 @@ def to_c_stencil(st: Stencil) -> _abi.bk_stencil:
     for t, (tap, c) in enumerate(zip(st.taps, st.coeff)):
         s.offsets[t][0], s.offsets[t][1], s.offsets[t][2] = tap
         s.coeff[t] = float(c)
+    s.pre_op, s.post_op = int(st.pre_op), int(st.post_op)
     return s
 
 

@@ -75,7 +75,7 @@ batch_sweep_kernel(const BatchDomain *__restrict__ doms, unsigned ndom, const ui
         const int lk = kk - R - qk * BK, lj = jj - R - qj * BJ, li = ii - R - qi * BI;
         const unsigned nb = nbr[(qk + 1) * 9 + (qj + 1) * 3 + (qi + 1)];
         const int o = RM ? (lk * BJ + lj) * BI + li : L.offset(lk, lj, li);
-        tile[e] = TileOf<T, ACC>::load(in + (size_t)nb * step + o);
+        tile[e] = op_apply(TileOf<T, ACC>::load(in + (size_t)nb * step + o), tp.pre);
       }
     }
     __syncthreads();
@@ -92,7 +92,7 @@ batch_sweep_kernel(const BatchDomain *__restrict__ doms, unsigned ndom, const ui
         if constexpr (ACC == ACCM_FF) v = stencil_point_ff<EJ, EI, R, FAM>(c, tp);
         else v = stencil_point<AT, EJ, EI, R, FAM, ACC>(c, tp);
         const int o = RM ? (k * BJ + j) * BI + i : L.offset(k, j, i);
-        Elem<T>::store(ob + o, v);
+        Elem<T>::store(ob + o, op_apply(v, tp.post));
       }
     }
     __syncthreads();

@@ -73,8 +73,13 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   plan->fam = fam;
   plan->r = fam == FAM_GENERIC ? GENERIC_R : r;
   plan->shape = shape_of(L);
+  if (st->pre_op < BK_OP_NONE || st->pre_op > BK_OP_ABS || st->post_op < BK_OP_NONE || st->post_op > BK_OP_ABS)
+    return fail(BK_ERR_ARG, "stencil pre_op / post_op must be BK_OP_NONE, BK_OP_RELU or BK_OP_ABS");
+  plan->ops = st->pre_op != BK_OP_NONE || st->post_op != BK_OP_NONE;
   if (!tp) return BK_OK;
   tp->n = n;
+  tp->pre = st->pre_op;
+  tp->post = st->post_op;
   static thread_local int offs[BK_MAX_TAPS][3];
   static thread_local int toff1[BK_MAX_TAPS];
   const int EJ = L.bj + 2 * GENERIC_R, EI = L.bi + 2 * GENERIC_R;
@@ -127,7 +132,7 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
     const size_t es = dtype_size(in->dtype);
     const size_t vb = (size_t)L.bi * es < 16 ? (size_t)L.bi * es : 16;
     const size_t ve = vb / es;
-    plan->v2 = plan->rm && (reinterpret_cast<uintptr_t>(in->dat) % 16 == 0) && in->step % ve == 0 &&
+    plan->v2 = plan->rm && !plan->ops && (reinterpret_cast<uintptr_t>(in->dat) % 16 == 0) && in->step % ve == 0 &&
                in->offset % ve == 0 && !getenv("BK_SWEEP_ONESHOT");
     // float-float cubes and the radius-4 star are bound by the FP32 pipes; the one-shot
     // kernel's single tile buffer keeps twice as many CTAs resident and wins there

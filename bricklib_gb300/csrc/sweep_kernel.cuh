@@ -40,6 +40,7 @@ struct SweepArgs {
 // Coefficients in kernel order; passed by value (kernel parameter constant bank).
 struct Taps {
   int n;
+  int pre, post;  // BK_OP_* applied to every input value / to the sum
   int toff[BK_MAX_TAPS];  // generic family: tap offset in tile elements from the centre
   float cf[BK_MAX_TAPS];   // coefficient rounded to float (the high part)
   float cl[BK_MAX_TAPS];   // float(c - cf): the low part, for float-float arithmetic
@@ -61,6 +62,23 @@ __device__ __forceinline__ void neumaier(AT &s, AT &comp, AT p) {
   const AT t = s + p;
   comp += (absval(s) >= absval(p)) ? ((s - t) + p) : ((p - t) + s);
   s = t;
+}
+
+// Pointwise operations of non-linear stencils (BK_OP_RELU = max(x, 0), BK_OP_ABS = |x|).
+// The FP64 versions work on the sign bit, so they do not occupy the FP64 pipe.
+__device__ __forceinline__ float op_apply(float x, int op) {
+  return op == BK_OP_RELU ? fmaxf(x, 0.0f) : (op == BK_OP_ABS ? fabsf(x) : x);
+}
+__device__ __forceinline__ double op_apply(double x, int op) {
+  const long long b = __double_as_longlong(x);
+  if (op == BK_OP_RELU) return b < 0 ? 0.0 : x;
+  if (op == BK_OP_ABS) return __longlong_as_double(b & 0x7FFFFFFFFFFFFFFFll);
+  return x;
+}
+__device__ __forceinline__ float2 op_apply(float2 x, int op) {  // hi carries the sign of hi + lo
+  if (op == BK_OP_RELU) return x.x < 0.0f ? make_float2(0.0f, 0.0f) : x;
+  if (op == BK_OP_ABS) return x.x < 0.0f ? make_float2(-x.x, -x.y) : x;
+  return x;
 }
 
 // ---------------------------------------------------------------- float-float (FP64 storage)
@@ -352,7 +370,7 @@ sweep_kernel(const SweepArgs a, const Taps tp) {
         const int lk = kk - R - qk * BK, lj = jj - R - qj * BJ, li = ii - R - qi * BI;
         const unsigned nb = nbr[(qk + 1) * 9 + (qj + 1) * 3 + (qi + 1)];
         const int o = RM ? (lk * BJ + lj) * BI + li : a.L.offset(lk, lj, li);
-        tile[e] = TileOf<T, ACC>::load(in + (size_t)nb * a.in_step + o);
+        tile[e] = op_apply(TileOf<T, ACC>::load(in + (size_t)nb * a.in_step + o), tp.pre);
       }
     }
     __syncthreads();
@@ -366,7 +384,7 @@ sweep_kernel(const SweepArgs a, const Taps tp) {
         if constexpr (ACC == ACCM_FF) v = stencil_point_ff<EJ, EI, R, FAM>(c, tp);
         else v = stencil_point<AT, EJ, EI, R, FAM, ACC>(c, tp);
         const int o = RM ? (k * BJ + j) * BI + i : a.L.offset(k, j, i);
-        Elem<T>::store(ob + o, v);
+        Elem<T>::store(ob + o, op_apply(v, tp.post));
       }
     }
     __syncthreads();
@@ -402,6 +420,7 @@ struct SweepPlan {
   int shape;  // 0: 8x8x8, 1: 4x4x4, 2: 16x8x8, 3: 8x8x32
   bool rm;
   bool v2;    // row-major and aligned: the pipelined kernel applies
+  bool ops;   // pointwise pre / post operations (one-shot kernels only)
   int fam;
   int r;
   int acc;

@@ -1,0 +1,193 @@
+"""Stencil-language front end: run a bricklib stencil script (the `.py` files the
+reference's code generator reads, e.g. stencils/7pt.py, stencils/mpi13pt.py) and lower the
+grid assigned in STENCIL to a tap list for bk_sweep.
+
+    st = load_stencil("stencils/mpi13pt.py", constants_from_header("stencils/fake.h"))
+    st = load_stencil("stencils/7pt.py", {"coeff": [c0, ..., c6]})
+
+Scripts import `st.expr`, `st.grid` and `st.func`; this package provides those modules,
+so a script runs unchanged (the reference resolves the same names in codegen/st).
+Lowering accepts expressions linear in the input grid -- sums of constant-times-reference
+terms, products by constants, negation, division by constants.  Taps keep the order in
+which the script first mentions them (the reference's summation order); repeated taps
+merge their coefficients.  The cond stencil's pattern -- max(x, 0) around every input
+reference and If(s > 0, s, -s) around the sum (stencils/cond.py) -- lowers to the sweep's
+pointwise pre / post operations; other non-linear scripts raise NotLinear.
+"""
+from __future__ import annotations
+
+import importlib
+import os
+import re
+import sys
+from typing import Dict, List, Optional, Tuple
+
+from .. import stencils
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class NotLinear(ValueError):
+    pass
+
+
+def _modules():
+    """The st package of this front end, importable under the names scripts use."""
+    mods = {}
+    if HERE not in sys.path:
+        sys.path.insert(0, HERE)
+    for name in ("st", "st.expr", "st.grid", "st.func"):
+        mods[name] = importlib.import_module(name)
+    return mods
+
+
+def constants_from_header(path: str) -> Dict[str, float]:
+    """`#define NAME number` lines of a C header (e.g. stencils/fake.h MPI_ALPHA ...)."""
+    out = {}
+    pat = re.compile(r"^\s*#\s*define\s+(\w+)\s+([-+0-9.eE]+)\s*$")
+    with open(path) as f:
+        for line in f:
+            m = pat.match(line)
+            if m:
+                try:
+                    out[m.group(1)] = float(m.group(2))
+                except ValueError:
+                    pass
+    return out
+
+
+def _const(name: str, consts: Dict) -> float:
+    try:
+        return float(name)
+    except ValueError:
+        pass
+    if name in consts:
+        return float(consts[name])
+    m = re.fullmatch(r"\s*(\w+)\s*\[\s*(\d+)\s*\]\s*", name)
+    if m and m.group(1) in consts:
+        return float(consts[m.group(1)][int(m.group(2))])
+    raise KeyError(f"no value for constant {name!r}")
+
+
+def _linear(e, consts, inp, order: List[Tuple[int, int, int]]):
+    """(constant term, {tap: coefficient}) of an expression linear in grid `inp`."""
+    ex = importlib.import_module("st.expr")
+    gr = importlib.import_module("st.grid")
+    if isinstance(e, ex.Lit):
+        return e.v, {}
+    if isinstance(e, ex.ConstRef):
+        return _const(e.name, consts), {}
+    if isinstance(e, gr.GridRef):
+        if e.grid is not inp:
+            raise NotLinear(f"reads grid {e.grid.name} besides the input")
+        o = e.offsets
+        tap = (o[2], o[1], o[0]) if len(o) == 3 else tuple(reversed(o))
+        if tap not in order:
+            order.append(tap)
+        return 0.0, {tap: 1.0}
+    if isinstance(e, ex.Op):
+        if e.op == "neg":
+            c, t = _linear(e.args[0], consts, inp, order)
+            return -c, {k: -v for k, v in t.items()}
+        a, b = e.args
+        ca, ta = _linear(a, consts, inp, order)
+        cb, tb = _linear(b, consts, inp, order)
+        if e.op in ("+", "-"):
+            s = 1.0 if e.op == "+" else -1.0
+            t = dict(ta)
+            for k, v in tb.items():
+                t[k] = t.get(k, 0.0) + s * v
+            return ca + s * cb, t
+        if e.op == "*":
+            if ta and tb:
+                raise NotLinear("product of two grid references")
+            if ta:
+                return ca * cb, {k: v * cb for k, v in ta.items()}
+            return ca * cb, {k: v * ca for k, v in tb.items()}
+        if e.op == "/":
+            if tb:
+                raise NotLinear("division by a grid reference")
+            return ca / cb, {k: v / cb for k, v in ta.items()}
+        raise NotLinear(f"operator {e.op}")
+    if isinstance(e, (ex.If, ex.Call)):
+        raise NotLinear(f"{type(e).__name__} is not a linear stencil")
+    raise NotLinear(f"unsupported node {type(e).__name__}")
+
+
+def _is_zero(e, consts) -> bool:
+    ex = importlib.import_module("st.expr")
+    try:
+        return (isinstance(e, ex.Lit) and e.v == 0.0) or (isinstance(e, ex.ConstRef) and _const(e.name, consts) == 0.0)
+    except KeyError:
+        return False
+
+
+def _strip_ops(expr, consts):
+    """Recognise the pointwise operations of the cond stencil (stencils/cond.py):
+    If(s > 0, s, -s) around the sum (post |.|) and max(x, 0) around every input reference
+    (pre max(., 0)).  Returns (expression without them, pre_op, post_op)."""
+    ex = importlib.import_module("st.expr")
+    gr = importlib.import_module("st.grid")
+    post = 0
+    if isinstance(expr, ex.If):
+        c = expr.cond
+        if (isinstance(c, ex.Op) and c.op == ">" and c.args[0] is expr.then and _is_zero(c.args[1], consts)
+                and isinstance(expr.other, ex.Op) and expr.other.op == "neg" and expr.other.args[0] is expr.then):
+            expr, post = expr.then, 2
+        else:
+            raise NotLinear("only If(s > 0, s, -s) (an absolute value) is supported")
+    found = {"relu": 0, "plain": 0}
+
+    def unwrap(e):
+        if isinstance(e, ex.Call):
+            if e.name == "max" and len(e.args) == 2 and isinstance(e.args[0], gr.GridRef) and _is_zero(e.args[1], consts):
+                found["relu"] += 1
+                return e.args[0]
+            raise NotLinear(f"function {e.name} is not supported")
+        if isinstance(e, gr.GridRef):
+            found["plain"] += 1
+            return e
+        if isinstance(e, ex.Op):
+            return ex.Op(e.op, *[unwrap(a) for a in e.args])
+        return e
+
+    expr = unwrap(expr)
+    if found["relu"] and found["plain"]:
+        raise NotLinear("max(x, 0) must wrap every input reference or none")
+    return expr, (1 if found["relu"] else 0), post
+
+
+def load_stencil(path: str, constants: Optional[Dict] = None, name: Optional[str] = None,
+                 input_grid: Optional[str] = None) -> stencils.Stencil:
+    """Run a stencil script and lower its (single) output grid to a Stencil."""
+    _modules()
+    ns: Dict = {"__name__": "__stencil__", "__file__": path}
+    with open(path) as f:
+        code = compile(f.read(), path, "exec")
+    exec(code, ns)
+    outs = ns.get("STENCIL")
+    if not outs:
+        raise ValueError(f"{path} defines no STENCIL")
+    if len(outs) != 1:
+        raise ValueError("one output grid per stencil is supported")
+    out = outs[0]
+    if out.assigned is None:
+        raise ValueError(f"output grid {out.name} is never assigned")
+    offs, expr = out.assigned
+    if any(offs):
+        raise ValueError("the output must be assigned at the centre (i, j, k)")
+    gr = importlib.import_module("st.grid")
+    grids = [v for v in ns.values() if isinstance(v, gr.Grid) and v is not out]
+    if input_grid:
+        grids = [g for g in grids if g.name == input_grid]
+    if len(grids) != 1:
+        raise ValueError("the script must declare exactly one input grid (or name it with input_grid)")
+    expr, pre, post = _strip_ops(expr, constants or {})
+    order: List[Tuple[int, int, int]] = []
+    c0, taps = _linear(expr, constants or {}, grids[0], order)
+    if c0 != 0.0:
+        raise NotLinear("affine term (a constant added to the stencil) is not supported")
+    order = [t for t in order if taps.get(t, 0.0) != 0.0]
+    st = stencils.custom(name or os.path.splitext(os.path.basename(path))[0], order, [taps[t] for t in order])
+    st.pre_op, st.post_op = pre, post
+    return st

@@ -56,6 +56,8 @@ class Stencil:
     taps: List[Tap]
     coeff: np.ndarray
     classes: List[int] = field(default_factory=list)  # symmetry class of each tap
+    pre_op: int = 0   # 0 none, 1 max(x, 0) on every input value
+    post_op: int = 0  # 0 none, 2 |sum|
 
     @property
     def npoints(self) -> int:
@@ -129,6 +131,11 @@ def make(name: str, seed: int = 0) -> Stencil:
         inv_h2 = 128.0 * 128.0
         c = np.array([-6.0 * inv_h2] + [inv_h2] * 6)
         return Stencil(name, taps, c, cls)
+    if name == "cond7":  # stencils/cond.py, 3axis.cpp:94-163: |sum c_t * max(x_t, 0)|, 3axis.cpp tap order
+        taps = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (0, 0, 0)]
+        cidx = [5, 6, 3, 4, 1, 2, 0]  # coeff[5] * in(k+1) + coeff[6] * in(k-1) + ...
+        c = uniform01(seed, 7)
+        return Stencil(name, taps, c[np.asarray(cidx)], list(range(7)), pre_op=1, post_op=2)
     raise ValueError(f"unknown stencil {name!r}")
 
 

@@ -134,7 +134,7 @@ inline bk_field brickField(const BrickT &b) {
 
 /// Tap-list builder: BrickStencil st; st.add(0,0,1, c1).add(0,0,-1, c2) ...
 struct BrickStencil : bk_stencil {
-  BrickStencil() { npoints = 0; }
+  BrickStencil() : bk_stencil() {}
   BrickStencil &add(int dk, int dj, int di, double c) {
     if (npoints < BK_MAX_TAPS) {
       offsets[npoints][0] = dk;

@@ -75,10 +75,20 @@ typedef struct bk_field {
  * The reference compiles each stencil from a Python script (stencils/7pt.py, mpi*.py)
  * into one kernel; here the tap list is data. |offset| on each axis must not exceed
  * the brick dim on that axis (the accessor reaches one neighbour brick, brick.h:232-245). */
+/* Pointwise operations around the weighted sum, for non-linear stencils such as the
+ * reference's cond kernel (stencils/cond.py, 3axis.cpp:94-163):
+ *   out = post( sum_t coeff[t] * pre(in(...)) )
+ * BK_OP_RELU is max(x, 0), BK_OP_ABS is |x|.  Both default to BK_OP_NONE (zero-filled). */
+#define BK_OP_NONE 0
+#define BK_OP_RELU 1
+#define BK_OP_ABS 2
+
 typedef struct bk_stencil {
   int npoints;
   int offsets[BK_MAX_TAPS][3];
   double coeff[BK_MAX_TAPS];
+  int pre_op;  /* applied to every input value */
+  int post_op; /* applied to the sum */
 } bk_stencil;
 
 /* ------------------------------------------------------------------ runtime */

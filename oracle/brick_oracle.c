@@ -171,11 +171,26 @@ static void tap_radius(int npts, const int *offs, int r[3]) {
 DEFINE_GATHER(gather_f64, double)
 DEFINE_GATHER(gather_f32, float)
 
+static inline double op_apply(double x, int op) {
+  if (op == 1) return x > 0.0 ? x : 0.0;  /* max(x, 0.0) */
+  if (op == 2) return x > 0 ? x : -x;     /* partial > 0 ? partial : -partial */
+  return x;
+}
+
 void orc_brick_sweep(const unsigned *adj, const double *in, long in_step, long in_off,
                      double *out, long out_step, long out_off,
                      const unsigned *blist, long nlist,
                      const int bdim[3], const int fold[3],
                      int npts, const int *offs, const double *coeff, int nthreads) {
+  orc_brick_sweep_ops(adj, in, in_step, in_off, out, out_step, out_off, blist, nlist, bdim, fold, npts, offs,
+                      coeff, 0, 0, nthreads);
+}
+
+void orc_brick_sweep_ops(const unsigned *adj, const double *in, long in_step, long in_off,
+                         double *out, long out_step, long out_off,
+                         const unsigned *blist, long nlist,
+                         const int bdim[3], const int fold[3],
+                         int npts, const int *offs, const double *coeff, int pre, int post, int nthreads) {
   int r[3];
   tap_radius(npts, offs, r);
   const int ek = bdim[0] + 2 * r[0], ej = bdim[1] + 2 * r[1], ei = bdim[2] + 2 * r[2];
@@ -190,6 +205,8 @@ void orc_brick_sweep(const unsigned *adj, const double *in, long in_step, long i
     for (long n = 0; n < nlist; ++n) {
       unsigned b = blist[n];
       gather_f64(adj, in, in_step, in_off, b, bdim, r, ot, tile);
+      if (pre)
+        for (long e = 0; e < (long)ek * ej * ei; ++e) tile[e] = op_apply(tile[e], pre);
       /* taps outermost, points inner: every point still sums its taps left to right */
       for (int t = 0; t < npts; ++t) {
         const double c = coeff[t];
@@ -205,7 +222,7 @@ void orc_brick_sweep(const unsigned *adj, const double *in, long in_step, long i
           }
       }
       double *ob = out + (size_t)b * out_step + out_off;
-      for (long p = 0; p < bs; ++p) ob[ot[p]] = acc[p];
+      for (long p = 0; p < bs; ++p) ob[ot[p]] = op_apply(acc[p], post);
     }
     free(tile);
     free(acc);
@@ -257,6 +274,12 @@ void orc_brick_sweep_f32(const unsigned *adj, const float *in, long in_step, lon
 void orc_array_sweep(const double *in, double *out, const long dims[3],
                      const long lo[3], const long hi[3],
                      int npts, const int *offs, const double *coeff, int nthreads) {
+  orc_array_sweep_ops(in, out, dims, lo, hi, npts, offs, coeff, 0, 0, nthreads);
+}
+
+void orc_array_sweep_ops(const double *in, double *out, const long dims[3],
+                         const long lo[3], const long hi[3],
+                         int npts, const int *offs, const double *coeff, int pre, int post, int nthreads) {
   const long sj = dims[2], sk = dims[1] * dims[2];
   if (nthreads <= 0) nthreads = orc_max_threads();
 #pragma omp parallel for collapse(2) schedule(static) num_threads(nthreads)
@@ -264,10 +287,10 @@ void orc_array_sweep(const double *in, double *out, const long dims[3],
     for (long j = lo[1]; j < hi[1]; ++j)
       for (long i = lo[2]; i < hi[2]; ++i) {
         const long p = k * sk + j * sj + i;
-        double v = coeff[0] * in[p + offs[0] * sk + offs[1] * sj + offs[2]];
+        double v = coeff[0] * op_apply(in[p + offs[0] * sk + offs[1] * sj + offs[2]], pre);
         for (int t = 1; t < npts; ++t)
-          v = v + coeff[t] * in[p + offs[3 * t] * sk + offs[3 * t + 1] * sj + offs[3 * t + 2]];
-        out[p] = v;
+          v = v + coeff[t] * op_apply(in[p + offs[3 * t] * sk + offs[3 * t + 1] * sj + offs[3 * t + 2]], pre);
+        out[p] = op_apply(v, post);
       }
 }
 

@@ -67,6 +67,14 @@ void orc_brick_sweep(const unsigned *adj, const double *in, long in_step, long i
                      const int bdim[3], const int fold[3],
                      int npts, const int *offs, const double *coeff, int nthreads);
 
+/* The same sweep for non-linear stencils: out = post(sum_t coeff[t] * pre(in)), op 0 none,
+ * 1 max(x, 0.0), 2 |x| written as x > 0 ? x : -x (the cond kernel, stencils/3axis.cpp:94-163). */
+void orc_brick_sweep_ops(const unsigned *adj, const double *in, long in_step, long in_off,
+                         double *out, long out_step, long out_off,
+                         const unsigned *blist, long nlist,
+                         const int bdim[3], const int fold[3],
+                         int npts, const int *offs, const double *coeff, int pre, int post, int nthreads);
+
 /* Same sweep, float storage with float accumulation in tap order (FP32 form). */
 void orc_brick_sweep_f32(const unsigned *adj, const float *in, long in_step, long in_off,
                          float *out, long out_step, long out_off,
@@ -80,6 +88,11 @@ void orc_brick_sweep_f32(const unsigned *adj, const float *in, long in_step, lon
 void orc_array_sweep(const double *in, double *out, const long dims[3],
                      const long lo[3], const long hi[3],
                      int npts, const int *offs, const double *coeff, int nthreads);
+
+/* Array sweep with pointwise operations (see orc_brick_sweep_ops). */
+void orc_array_sweep_ops(const double *in, double *out, const long dims[3],
+                         const long lo[3], const long hi[3],
+                         int npts, const int *offs, const double *coeff, int pre, int post, int nthreads);
 
 /* Periodic ghost fill of a padded array: every cell of the box
  * org - ghost .. org + n + ghost - 1 outside the interior org .. org + n - 1 gets the

@@ -55,6 +55,11 @@ def lib():
         L.orc_brick_sweep_f32.argtypes = [_u32p, _f32p, C.c_long, C.c_long, _f32p, C.c_long, C.c_long,
                                           _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int]
         L.orc_array_sweep.argtypes = [_f64p, _f64p, _l3, _l3, _l3, C.c_int, _i32p, _f64p, C.c_int]
+        L.orc_brick_sweep_ops.argtypes = [_u32p, _f64p, C.c_long, C.c_long, _f64p, C.c_long, C.c_long,
+                                          _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int, C.c_int,
+                                          C.c_int]
+        L.orc_array_sweep_ops.argtypes = [_f64p, _f64p, _l3, _l3, _l3, C.c_int, _i32p, _f64p, C.c_int, C.c_int,
+                                          C.c_int]
         L.orc_array_periodic_fill.argtypes = [_f64p, _l3, _l3, _l3, _l3]
         L.orc_periodic_plan.argtypes = [_u32p, _l3, _l3, C.c_void_p]
         L.orc_periodic_plan.restype = C.c_long
@@ -75,6 +80,7 @@ def ref() -> Optional[C.CDLL]:
         R.ref_layout_offsets.argtypes = [C.c_int, _i64p]
         R.ref_init_grid.argtypes = [C.c_long, C.c_long, C.c_long, _u32p, _u32p]
         R.ref_sweep.argtypes = [C.c_int, C.c_long, _f64p, C.c_int, _i32p, _f64p, _f64p, _f64p]
+        R.ref_cond.argtypes = [C.c_long, _f64p, _f64p, _f64p, _f64p]
         _ref = R
     return _ref
 
@@ -111,19 +117,25 @@ def copy_brick(to_brick: bool, dim, pad, ghost, arr: np.ndarray, grid: np.ndarra
 
 
 def brick_sweep(adj, inp, in_step, in_off, out, out_step, out_off, blist, bdim, fold,
-                offs: np.ndarray, coeff: np.ndarray, nthreads: int = 0) -> None:
+                offs: np.ndarray, coeff: np.ndarray, nthreads: int = 0, pre: int = 0, post: int = 0) -> None:
     offs = np.ascontiguousarray(offs, dtype=np.int32).reshape(-1)
     coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+    if pre or post:
+        lib().orc_brick_sweep_ops(adj, inp.reshape(-1), in_step, in_off, out.reshape(-1), out_step, out_off,
+                                  blist, len(blist), _i3(*bdim), _i3(*fold), len(coeff), offs, coeff, pre, post,
+                                  nthreads)
+        return
     fn = lib().orc_brick_sweep if inp.dtype == np.float64 else lib().orc_brick_sweep_f32
     fn(adj, inp.reshape(-1), in_step, in_off, out.reshape(-1), out_step, out_off,
        blist, len(blist), _i3(*bdim), _i3(*fold), len(coeff), offs, coeff, nthreads)
 
 
-def array_sweep(inp: np.ndarray, out: np.ndarray, lo, hi, offs, coeff, nthreads: int = 0) -> None:
+def array_sweep(inp: np.ndarray, out: np.ndarray, lo, hi, offs, coeff, nthreads: int = 0,
+                pre: int = 0, post: int = 0) -> None:
     offs = np.ascontiguousarray(offs, dtype=np.int32).reshape(-1)
     coeff = np.ascontiguousarray(coeff, dtype=np.float64)
-    lib().orc_array_sweep(inp.reshape(-1), out.reshape(-1), _l3(*inp.shape), _l3(*lo), _l3(*hi),
-                          len(coeff), offs, coeff, nthreads)
+    lib().orc_array_sweep_ops(inp.reshape(-1), out.reshape(-1), _l3(*inp.shape), _l3(*lo), _l3(*hi),
+                              len(coeff), offs, coeff, pre, post, nthreads)
 
 
 def array_periodic_fill(a: np.ndarray, org, n, ghost) -> None:

@@ -104,6 +104,58 @@ int sweep(long n, const double *in_arr, int npts, const int *offs, const double 
   return ok ? 1 : 0;
 }
 
+// The cond kernel of stencils/3axis.cpp:94-163 (d3cond): array and accessor brick versions
+// with the reference's expression, coeff[0..6] in its order.
+int cond_sweep(long n, const double *in_arr, const double *coeff, double *out_brick, double *out_arr) {
+  typedef Brick<Dim<8, 8, 8>, Dim<4, 8>> B;
+  const long STRIDE = n + 2 * (GZ + PADDING), STRIDEG = n + 2 * GZ, gb = STRIDEG / 8;
+  const long sz = STRIDE * STRIDE * STRIDE;
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<3>(grid_ptr, {gb, gb, gb});
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, 1024);
+  B bIn(&bInfo, bStorage, 0), bOut(&bInfo, bStorage, 512);
+  std::memset(bStorage.dat.get(), 0, sizeof(bElem) * bStorage.chunks * bStorage.step);
+  bElem *in_ptr = (bElem *)aligned_alloc(ALIGN, sizeof(bElem) * sz);
+  std::memcpy(in_ptr, in_arr, sizeof(bElem) * sz);
+  copyToBrick<3>({STRIDEG, STRIDEG, STRIDEG}, {PADDING, PADDING, PADDING}, {0, 0, 0}, in_ptr, grid_ptr, bIn);
+  auto arr_in = (bElem(*)[STRIDE][STRIDE])in_ptr;
+  auto arr_out = (bElem(*)[STRIDE][STRIDE])out_arr;
+  std::memset(out_arr, 0, sizeof(bElem) * sz);
+  using std::max;
+  for (long k = PADDING; k < PADDING + STRIDEG; ++k)
+    for (long j = PADDING; j < PADDING + STRIDEG; ++j)
+      for (long i = PADDING; i < PADDING + STRIDEG; ++i) {
+        bElem partial = coeff[5] * max(arr_in[k + 1][j][i], 0.0) + coeff[6] * max(arr_in[k - 1][j][i], 0.0) +
+                        coeff[3] * max(arr_in[k][j + 1][i], 0.0) + coeff[4] * max(arr_in[k][j - 1][i], 0.0) +
+                        coeff[1] * max(arr_in[k][j][i + 1], 0.0) + coeff[2] * max(arr_in[k][j][i - 1], 0.0) +
+                        coeff[0] * max(arr_in[k][j][i], 0.0);
+        arr_out[k][j][i] = partial > 0 ? partial : -partial;
+      }
+  auto grid = (unsigned(*)[gb][gb])grid_ptr;
+  for (long tk = 1; tk < gb - 1; ++tk)
+    for (long tj = 1; tj < gb - 1; ++tj)
+      for (long ti = 1; ti < gb - 1; ++ti) {
+        unsigned b = grid[tk][tj][ti];
+        for (long k = 0; k < 8; ++k)
+          for (long j = 0; j < 8; ++j)
+            for (long i = 0; i < 8; ++i) {
+              bElem partial =
+                  coeff[5] * max(bIn[b][k + 1][j][i], 0.0) + coeff[6] * max(bIn[b][k - 1][j][i], 0.0) +
+                  coeff[3] * max(bIn[b][k][j + 1][i], 0.0) + coeff[4] * max(bIn[b][k][j - 1][i], 0.0) +
+                  coeff[1] * max(bIn[b][k][j][i + 1], 0.0) + coeff[2] * max(bIn[b][k][j][i - 1], 0.0) +
+                  coeff[0] * max(bIn[b][k][j][i], 0.0);
+              bOut[b][k][j][i] = partial > 0 ? partial : -partial;
+            }
+      }
+  bool ok = compareBrick<3>({n, n, n}, {PADDING, PADDING, PADDING}, {GZ, GZ, GZ}, out_arr, grid_ptr, bOut);
+  std::memset(out_brick, 0, sizeof(bElem) * sz);
+  copyFromBrick<3>({n, n, n}, {PADDING, PADDING, PADDING}, {GZ, GZ, GZ}, out_brick, grid_ptr, bOut);
+  free(in_ptr);
+  free(grid_ptr);
+  free(bInfo.adj);
+  return ok ? 1 : 0;
+}
+
 typedef Lay<8, 8, 8, Dim<4, 8>> L0;     // CUDA fold (stencils/cudavfold.h:9)
 typedef Lay<8, 8, 8, Dim<8>> L1;        // AVX-512 fold (stencils/cpuvfold.h:12-13)
 typedef Lay<8, 8, 8, Dim<2, 2>> L2;     // docs/usingbricks.md example fold
@@ -151,6 +203,11 @@ int ref_sweep(int layout, long n, const double *in_arr, int npts, const int *off
     case 4: return sweep<L4>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
   }
   return -1;
+}
+
+/* The reference's cond kernel (3axis.cpp:94-163) on an n^3 interior; coeff[0..6]. */
+int ref_cond(long n, const double *in_arr, const double *coeff, double *out_brick, double *out_arr) {
+  return cond_sweep(n, in_arr, coeff, out_brick, out_arr);
 }
 
 }  // extern "C"

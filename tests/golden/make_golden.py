@@ -8,7 +8,8 @@ Fixtures written:
   layouts.npz       in-brick element offsets computed by the reference accessor
                     (include/brick.h:213-327) for seven brick-dims / vector-fold pairs
   init_grid.npz     grid and adjacency of init_grid<3> (include/bricksetup.h:73-90) on 5x4x3
-  sweep_<shape>.npz one sweep on a 16^3 interior (+8 ghost, +8 padding) through
+  sweep_<shape>.npz one sweep on a 16^3 interior (sweep_cond7: the reference's cond kernel,
+                    |sum coeff * max(x, 0)|, stencils/3axis.cpp:94-163) (+8 ghost, +8 padding) through
                     copyToBrick -> accessor brick kernel -> compareBrick -> copyFromBrick,
                     input uniform[-1,1) from splitmix64 seed 1234: the interior output,
                     the max |brick - array| difference and the reference's compareBrick verdict
@@ -79,6 +80,19 @@ def main():
                  ref_match=ok, n=N, seed_in=SEED_IN, seed_coeff=SEED_COEFF, layout=lid,
                  offsets=st.offsets(), coeff=st.coeff, input_sum=inp.sum())
         print(f"{tag:22s} compareBrick={ok} max|brick-array|={np.max(np.abs(ob - oa)):.3e}")
+
+    # the cond kernel (3axis.cpp:94-163): coeff[0..6] as the reference indexes them
+    coeff = stencils.uniform01(SEED_COEFF, 7)
+    ob = np.zeros(S * S * S)
+    oa = np.zeros(S * S * S)
+    ok = R.ref_cond(N, inp, coeff, ob, oa)
+    ob = ob.reshape(S, S, S)[16:16 + N, 16:16 + N, 16:16 + N].copy()
+    oa = oa.reshape(S, S, S)[16:16 + N, 16:16 + N, 16:16 + N].copy()
+    st = stencils.make("cond7", SEED_COEFF)
+    np.savez(os.path.join(OUT, "sweep_cond7.npz"), out=ob, arr_maxdiff=np.max(np.abs(ob - oa)),
+             ref_match=ok, n=N, seed_in=SEED_IN, seed_coeff=SEED_COEFF, layout=0,
+             offsets=st.offsets(), coeff=st.coeff, input_sum=inp.sum(), pre_op=1, post_op=2)
+    print(f"{'cond7':22s} compareBrick={ok} max|brick-array|={np.max(np.abs(ob - oa)):.3e}")
 
 
 if __name__ == "__main__":

@@ -71,6 +71,8 @@ def oracle_array(dom, arr, st):
 def test_fp64_matches_reference_golden(path):
     z = np.load(path)
     st = stencils.custom("golden", [tuple(t) for t in z["offsets"]], z["coeff"])
+    st.pre_op = int(z["pre_op"]) if "pre_op" in z else 0
+    st.post_op = int(z["post_op"]) if "post_op" in z else 0
     lay = B.Layout((8, 8, 8), (1, 4, 8)) if int(z["layout"]) == 0 else B.Layout((4, 4, 4), (1, 4, 4))
     _, _, got = device_sweep(int(z["n"]), st, layout=lay, seed=int(z["seed_in"]))
     ok, md = mixed_ok(got, z["out"])
@@ -267,3 +269,28 @@ def test_floatfloat_rejected_for_fp32():
         B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, stencils.make("star7", 1),
                      _abi.BK_ACC_FLOATFLOAT)
     assert e.value.status == _abi.BK_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("dtype,acc,tol", [(BK_F64, BK_ACC_NATIVE, 1e-14), (BK_F64, _abi.BK_ACC_FLOATFLOAT, 1e-12),
+                                           (BK_F32, BK_ACC_NATIVE, 1e-5)])
+def test_cond_stencil_against_oracle(dtype, acc, tol):
+    """The non-linear cond kernel (|sum c * max(x, 0)|) in every storage / arithmetic mode."""
+    st = stencils.make("cond7", 3)
+    dom, arr, got = device_sweep(32, st, dtype=dtype, acc=acc, seed=12)
+    ref = np.zeros_like(arr)
+    o, n = dom.org, dom.n
+    src = arr.astype(np.float32).astype(np.float64) if dtype == BK_F32 else arr
+    oracle.array_sweep(src, ref, o, tuple(a + b for a, b in zip(o, n)), st.offsets(), st.coeff,
+                       pre=st.pre_op, post=st.post_op)
+    ref = dom.interior_view(ref)
+    assert np.all(got >= 0)
+    assert normwise(got, ref) <= tol
+
+
+def test_dsl_script_runs_on_the_gpu():
+    from bricklib_gb300 import dsl
+    path = os.path.join(os.path.dirname(__file__), "golden", "dsl", "star13_loops.py")
+    st = dsl.load_stencil(path, {"W0": 0.4, "W1": 0.07, "W2": 0.03})
+    dom, arr, got = device_sweep(32, st, seed=21)
+    ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+    assert ok, md

@@ -51,15 +51,17 @@ def test_brick_sweep_matches_golden(path):
     assert inp.sum() == float(z["input_sum"])
     dat = dom.alloc()
     dom.to_bricks(inp, dat, 0)
+    pre = int(z["pre_op"]) if "pre_op" in z else 0
+    post = int(z["post_op"]) if "post_op" in z else 0
     oracle.brick_sweep(dom.adj, dat, dom.step, 0, dat, dom.step, dom.bsize, dom.interior,
-                       bdim, fold, z["offsets"], z["coeff"])
+                       bdim, fold, z["offsets"], z["coeff"], pre=pre, post=post)
     got = dom.interior_view(dom.from_bricks(dat, dom.bsize))
     # same taps, same order, separately rounded doubles: bit-identical
     np.testing.assert_array_equal(got, z["out"])
     # array oracle over the same interior
     out = np.zeros_like(inp)
     o = dom.ghost + dom.pad
-    oracle.array_sweep(inp, out, (o, o, o), (o + n, o + n, o + n), z["offsets"], z["coeff"])
+    oracle.array_sweep(inp, out, (o, o, o), (o + n, o + n, o + n), z["offsets"], z["coeff"], pre=pre, post=post)
     np.testing.assert_array_equal(dom.interior_view(out), z["out"])
     bad, maxdiff, _ = dom.compare(out, dat, dom.bsize, 1e-12)
     assert bad == 0 and maxdiff == 0.0
