@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "batch_common.cuh"
+#include "sweep2_kernel.cuh"
 
 namespace bk {
 
@@ -146,8 +147,44 @@ int launch_batch_sweep(const BatchDomain *doms, unsigned ndom, const uint2 *work
 
 template <typename T, int ACC>
 int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndom, const uint2 *work, unsigned nwork,
-                   int parity, const Layout &L, int *err, int grid_cap, cudaStream_t s) {
+                   int parity, const Layout &L, int *err, int grid_cap, bool aligned, cudaStream_t s) {
   const SweepPlan &p = bs.plan;
+  // the pipelined kernel in batch mode for row-major layouts and aligned fields (every field
+  // base is 16-byte aligned when the storages come from cudaMalloc and offsets are whole
+  // bricks); the one-shot batch kernel below serves the rest
+  const bool v2 = aligned && p.rm && !p.ops && !(ACC == ACCM_FF && (p.fam == FAM_CUBE || p.r >= 4)) &&
+                  !getenv("BK_SWEEP_ONESHOT");
+  if (v2) {
+    SweepArgs a{};
+    a.nlist = nwork;
+    a.err = err;
+    a.L = L;
+    a.doms = doms;
+    a.work = work;
+    a.ndom = ndom;
+    a.parity = parity;
+    Taps &tp = const_cast<Taps &>(bs.taps);
+#define BK_B2(BK_, BJ_, BI_, R_, FAM_)                                                        \
+  if (p.r == R_ && p.fam == FAM_) {                                                          \
+    if (FAM_ == FAM_GENERIC) {                                                               \
+      typedef Sweep2Geom<T, BK_, BJ_, BI_, R_> G;                                            \
+      for (int t = 0; t < tp.n; ++t)                                                         \
+        tp.toff[t] = (p.offs[t][0] * G::EJ + p.offs[t][1]) * G::EI + p.offs[t][2];           \
+    }                                                                                        \
+    return launch_sweep2<T, BK_, BJ_, BI_, R_, FAM_, ACC, true>(a, tp, s, grid_cap);         \
+  }
+#define BK_B2SET(BK_, BJ_, BI_)                                                               \
+  BK_B2(BK_, BJ_, BI_, 1, FAM_STAR) BK_B2(BK_, BJ_, BI_, 2, FAM_STAR) BK_B2(BK_, BJ_, BI_, 4, FAM_STAR) \
+  BK_B2(BK_, BJ_, BI_, 1, FAM_CUBE) BK_B2(BK_, BJ_, BI_, 2, FAM_CUBE)
+    if (p.shape == 0) { BK_B2SET(8, 8, 8) }
+    if constexpr (ACC == ACCM_NATIVE && sizeof(T) == 4) {
+      if (p.shape == 1) { BK_B2SET(4, 4, 4) }
+      if (p.shape == 2) { BK_B2SET(16, 8, 8) }
+      if (p.shape == 3) { BK_B2SET(8, 8, 32) }
+    }
+#undef BK_B2SET
+#undef BK_B2
+  }
 #define BK_BC(BK_, BJ_, BI_, R_, FAM_, RM_)                                                              \
   if (p.r == R_ && p.fam == FAM_ && p.rm == RM_)                                                         \
     return launch_batch_sweep<T, BK_, BJ_, BI_, R_, FAM_, RM_, ACC>(doms, ndom, work, nwork, parity, bs.taps, L, \
@@ -187,6 +224,7 @@ struct bk_batch {
   std::vector<std::pair<unsigned, unsigned>> seg;  // per stencil: (first work item, count)
   int parity = 0;
   int grid_cap = 0;
+  bool aligned = true;  // every field base and step 16-byte aligned: the pipelined kernel applies
   int *err = nullptr;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, fill, parity) -> graph
 };
@@ -198,15 +236,16 @@ int plan_stencil(const bk_stencil *st, const Layout &L, int dtype, int acc, Swee
 // Launchers shared with the server (serve.cu): one stencil over a work segment, and the
 // batched ghost fill.
 int batch_launch_sweep(const BatchStencil &bs, int dtype, const BatchDomain *doms, unsigned ndom, const uint2 *work,
-                       unsigned nwork, int parity, const Layout &L, int *err, int grid_cap, cudaStream_t s) {
+                       unsigned nwork, int parity, const Layout &L, int *err, int grid_cap, bool aligned,
+                       cudaStream_t s) {
   if (!nwork) return BK_OK;
   const int acc = bs.plan.acc;
   if (dtype == BK_F32)
-    return acc == ACCM_COMP ? batch_dispatch<float, ACCM_COMP>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s)
-                            : batch_dispatch<float, ACCM_NATIVE>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s);
+    return acc == ACCM_COMP ? batch_dispatch<float, ACCM_COMP>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, aligned, s)
+                            : batch_dispatch<float, ACCM_NATIVE>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, aligned, s);
   if (dtype == BK_F64)
-    return acc == ACCM_FF ? batch_dispatch<double, ACCM_FF>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s)
-                          : batch_dispatch<double, ACCM_NATIVE>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, s);
+    return acc == ACCM_FF ? batch_dispatch<double, ACCM_FF>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, aligned, s)
+                          : batch_dispatch<double, ACCM_NATIVE>(bs, doms, ndom, work, nwork, parity, L, err, grid_cap, aligned, s);
   return fail(BK_ERR_UNSUPPORTED, "batch: BF16 storage is not instantiated");
 }
 
@@ -228,15 +267,8 @@ static int batch_sweep(bk_batch *b, cudaStream_t s) {
     const unsigned first = b->seg[q].first, count = b->seg[q].second;
     if (!count) continue;
     const uint2 *work = b->d_work + first;
-    int st;
-    if (b->dtype == BK_F32)
-      st = b->acc == ACCM_COMP ? batch_dispatch<float, ACCM_COMP>(b->sts[q], b->d_doms, b->ndom, work, count, b->parity, b->L, b->err, b->grid_cap, s)
-                               : batch_dispatch<float, ACCM_NATIVE>(b->sts[q], b->d_doms, b->ndom, work, count, b->parity, b->L, b->err, b->grid_cap, s);
-    else if (b->dtype == BK_F64)
-      st = b->acc == ACCM_FF ? batch_dispatch<double, ACCM_FF>(b->sts[q], b->d_doms, b->ndom, work, count, b->parity, b->L, b->err, b->grid_cap, s)
-                             : batch_dispatch<double, ACCM_NATIVE>(b->sts[q], b->d_doms, b->ndom, work, count, b->parity, b->L, b->err, b->grid_cap, s);
-    else
-      st = fail(BK_ERR_UNSUPPORTED, "batch: BF16 storage is not instantiated");
+    const int st = batch_launch_sweep(b->sts[q], b->dtype, b->d_doms, b->ndom, work, count, b->parity, b->L, b->err,
+                                      b->grid_cap, b->aligned, s);
     if (st) return st;
   }
   return BK_OK;
@@ -306,6 +338,7 @@ int bk_batch_create(bk_batch **out, const bk_batch_domain *doms, unsigned ndom, 
     }
     unsigned char *base = reinterpret_cast<unsigned char *>(D.dat);
     hd[d] = BatchDomain{D.adj, D.nbricks, (unsigned)D.stencil, base + D.off0 * es, base + D.off1 * es, D.step * es, D.chunks};
+    if ((reinterpret_cast<uintptr_t>(base) | (D.off0 * es) | (D.off1 * es) | (D.step * es)) % 16) b->aligned = false;
     for (unsigned n = 0; n < D.nlist; ++n) per_st[D.stencil].push_back(make_uint2(d, D.blist[n]));
     for (unsigned p = 0; p < D.npairs; ++p) pairs.push_back(make_uint3(d, D.pairs[2 * p], D.pairs[2 * p + 1]));
   }

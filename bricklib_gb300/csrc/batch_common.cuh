@@ -7,14 +7,6 @@ namespace bk {
 
 constexpr int BATCH_MAX_ST = 8;
 
-struct BatchDomain {  // device table entry
-  const unsigned *adj;
-  unsigned nbricks;
-  unsigned stencil;
-  unsigned char *f0, *f1;  // field bases (dat + offset), bytes
-  unsigned long long step_bytes;
-  long long chunks;
-};
 
 // What one per-stencil launch needs besides the work segment.
 struct BatchStencil {
@@ -24,7 +16,8 @@ struct BatchStencil {
 
 int plan_stencil(const bk_stencil *st, const Layout &L, int dtype, int acc, SweepPlan *plan, Taps *tp);
 int batch_launch_sweep(const BatchStencil &bs, int dtype, const BatchDomain *doms, unsigned ndom, const uint2 *work,
-                       unsigned nwork, int parity, const Layout &L, int *err, int grid_cap, cudaStream_t s);
+                       unsigned nwork, int parity, const Layout &L, int *err, int grid_cap, bool aligned,
+                       cudaStream_t s);
 int batch_launch_fill(const BatchDomain *doms, unsigned ndom, const uint3 *pairs, unsigned npairs, int parity,
                       size_t brick_bytes, int *err, cudaStream_t s);
 

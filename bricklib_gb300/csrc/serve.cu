@@ -397,8 +397,9 @@ static int tick(bk_server *S) {
   }
   for (auto &ws : S->work_seg) {
     const Group &g = S->groups[ws.first];
+    // job storages come from cudaMallocAsync and hold two whole-brick fields: aligned
     int st = batch_launch_sweep(g.bs, g.dtype, S->d_doms, S->ndom, S->d_work + ws.second.first, ws.second.second,
-                                S->parity, S->L, S->err, 0, s);
+                                S->parity, S->L, S->err, 0, true, s);
     if (st) return st;
   }
   S->parity ^= 1;

@@ -99,7 +99,7 @@ struct Sweep2Cfg {
   // float-float converts each raw FP64 tile into float pairs in place (same 8 bytes)
   static constexpr int FTILE_BYTES = 0;
   // bricks per CTA: as many as fit 128 threads and a ~100 KB shared-memory budget
-  static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 28 * 4;
+  static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 36 * 4;
   static constexpr int NB = cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
   static constexpr int NT = TPB * NB;
   static constexpr int SMEM = NB * PER_BRICK;
@@ -179,7 +179,7 @@ __device__ __forceinline__ unsigned plan_entry(int g) {
   return slot | (src << 5) | (dst << 18);
 }
 
-template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH>
 __global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC>::NT)
 sweep2_kernel(const SweepArgs a, const Taps tp) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
@@ -191,14 +191,13 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
   unsigned char *raw1 = smem_raw + NB * C::TILE_BYTES;          // [NB] tiles, buffer 1
   unsigned *nbrs = reinterpret_cast<unsigned *>(smem_raw + 2 * NB * C::TILE_BYTES + NB * C::FTILE_BYTES);
+  // nbrs slot (36 words): [0..26] adjacency, [27] active, [28..29] input field base,
+  // [30..31] output field base, [32..33] / [34..35] input / output storage step (elements)
   // nbrs: [3][NB][28]: adjacency of the groups being computed, copied and staged
   // (three slots, so staging the group after next never overwrites one still read);
   // entry [27] is the brick's active flag
 
   const int slot = threadIdx.x / TPB, lt = threadIdx.x - slot * TPB;
-  const T *in = reinterpret_cast<const T *>(a.in) + a.in_off;
-  T *out = reinterpret_cast<T *>(a.out) + a.out_off;
-
   unsigned plan[EPT];
 #pragma unroll
   for (int e = 0; e < EPT; ++e) {
@@ -208,40 +207,93 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
 
-  // stage the adjacency of group `grp` into nbrs[ns]
-  auto load_adj = [&](long long grp, int ns) {
-    unsigned *nbr = nbrs + (ns * NB + slot) * 28;
+  // Adjacency of a group: fetched into registers two groups ahead (its global-load latency
+  // hides under the current group's compute), stored into one of three nbrs slots.
+  constexpr int APT = (27 + TPB - 1) / TPB;  // adjacency entries per thread
+  unsigned av[APT];
+  int aok[APT];
+  unsigned long long fin = 0, fout = 0, fsin = 0, fsout = 0;  // held by the thread of slot 13
+  auto fetch_adj = [&](long long grp) {
     const long long n = grp * NB + slot;
-    for (int sl = lt; sl < 27; sl += TPB) {
+#pragma unroll
+    for (int q = 0; q < APT; ++q) {
+      const int sl = lt + q * TPB;
       unsigned v = 0;
       int ok = 0;
-      if (grp < ngroups && n < a.nlist) {
-        const unsigned b = a.blist[n];
-        if (b < a.nbricks) {
-          v = a.adj[(size_t)b * 27 + sl];
+      if (sl < 27 && grp < ngroups && n < a.nlist) {
+        const unsigned *adj;
+        unsigned b, nbricks;
+        long long in_chunks, out_chunks;
+        if constexpr (BATCH) {
+          const uint2 w = a.work[n];
+          const bool dok = w.x < a.ndom;
+          const BatchDomain &D = a.doms[dok ? w.x : 0];
+          adj = D.adj;
+          b = dok ? w.y : 0xFFFFFFFFu;
+          nbricks = D.nbricks;
+          in_chunks = out_chunks = D.chunks;
+          if (sl == 13) {
+            fin = reinterpret_cast<unsigned long long>(a.parity ? D.f1 : D.f0);
+            fout = reinterpret_cast<unsigned long long>(a.parity ? D.f0 : D.f1);
+            fsin = fsout = D.step_bytes / sizeof(T);
+          }
+        } else {
+          adj = a.adj;
+          b = a.blist[n];
+          nbricks = a.nbricks;
+          in_chunks = a.in_chunks;
+          out_chunks = a.out_chunks;
+          if (sl == 13) {
+            fin = reinterpret_cast<unsigned long long>(reinterpret_cast<const T *>(a.in) + a.in_off);
+            fout = reinterpret_cast<unsigned long long>(reinterpret_cast<T *>(a.out) + a.out_off);
+            fsin = a.in_step;
+            fsout = a.out_step;
+          }
+        }
+        if (b < nbricks) {
+          v = adj[(size_t)b * 27 + sl];
           ok = 1;
-          if (sl == 13 && ((long long)v >= a.out_chunks || (long long)v >= a.in_chunks)) ok = 0;
-          if ((long long)v >= a.in_chunks || !ok) { atomicOr(a.err, FLAG_BOUNDS); v = 0; }
+          if (sl == 13 && ((long long)v >= out_chunks || (long long)v >= in_chunks)) ok = 0;
+          if ((long long)v >= in_chunks || !ok) { atomicOr(a.err, FLAG_BOUNDS); v = 0; }
         } else if (sl == 13) {
           atomicOr(a.err, FLAG_BOUNDS);
         }
       }
-      nbr[sl] = v;
-      if (sl == 13) nbr[27] = ok;
+      av[q] = v;
+      aok[q] = ok;
+    }
+  };
+  auto store_adj = [&](int ns) {
+    unsigned *nbr = nbrs + (ns * NB + slot) * 36;
+#pragma unroll
+    for (int q = 0; q < APT; ++q) {
+      const int sl = lt + q * TPB;
+      if (sl < 27) {
+        nbr[sl] = av[q];
+        if (sl == 13) {
+          nbr[27] = aok[q];
+          *reinterpret_cast<unsigned long long *>(nbr + 28) = fin;
+          *reinterpret_cast<unsigned long long *>(nbr + 30) = fout;
+          *reinterpret_cast<unsigned long long *>(nbr + 32) = fsin;
+          *reinterpret_cast<unsigned long long *>(nbr + 34) = fsout;
+        }
+      }
     }
   };
   // issue the asynchronous gather of the group staged in nbrs[ns] into raw buffer buf
   auto issue = [&](int buf, int ns) {
-    const unsigned *nbr = nbrs + (ns * NB + slot) * 28;
+    const unsigned *nbr = nbrs + (ns * NB + slot) * 36;
     if (nbr[27]) {
       unsigned char *tile = (buf ? raw1 : raw0) + slot * C::TILE_BYTES;
       const unsigned tbase = smem_u32(tile);
+      const T *in = reinterpret_cast<const T *>(*reinterpret_cast<const unsigned long long *>(nbr + 28));
+      const size_t step = *reinterpret_cast<const unsigned long long *>(nbr + 32);
 #pragma unroll
       for (int e = 0; e < EPT; ++e) {
         const unsigned p = plan[e];
         if (p != 0xFFFFFFFFu) {
           const unsigned sl = p & 31u, src = (p >> 5) & 8191u, dst = p >> 18;
-          const T *g = in + (size_t)nbr[sl] * a.in_step + src;
+          const T *g = in + (size_t)nbr[sl] * step + src;
           cp_async<C::VB>(tbase + dst * C::ES, g);
         }
       }
@@ -249,21 +301,25 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     cp_async_commit();
   };
 
+  // prologue: adjacency of the first two groups, copies of the first
   long long grp = blockIdx.x;
-  load_adj(grp, 0);
+  fetch_adj(grp);
+  store_adj(0);
+  fetch_adj(grp + gridDim.x);
+  store_adj(1);
   __syncthreads();
   issue(0, 0);
 
   for (int it = 0; grp < ngroups; grp += gridDim.x, ++it) {
     const int cur = it & 1, nxt = cur ^ 1;
-    const int ncur = it % 3, nnxt = (it + 1) % 3;
-    load_adj(grp + gridDim.x, nnxt);
-    __syncthreads();  // nbrs[nnxt] visible; every thread is done with raw[nxt]
+    const int ncur = it % 3, nnxt = (it + 1) % 3, nfar = (it + 2) % 3;
+    __syncthreads();     // nbrs[nnxt] visible; every thread is done with raw[nxt] and nbrs[nfar]
     issue(nxt, nnxt);
+    fetch_adj(grp + 2ll * gridDim.x);  // lands while this group computes
     cp_async_wait<1>();  // this thread's copies for the current group have landed
     __syncthreads();     // ... and everybody else's
 
-    const unsigned *nbr = nbrs + (ncur * NB + slot) * 28;
+    const unsigned *nbr = nbrs + (ncur * NB + slot) * 36;
     const bool active = nbr[27] != 0;
     const T *rt = reinterpret_cast<const T *>((cur ? raw1 : raw0) + slot * C::TILE_BYTES);
     if constexpr (ACC == ACCM_FF) {
@@ -277,7 +333,9 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
       int j = lt / BI;
       const int i = lt - j * BI;
       if (C::PERM) j = (j & ~3) | ((j & 1) << 1) | ((j >> 1) & 1);  // rows 0,2,1,3 per warp
-      T *ob = out + (size_t)nbr[13] * a.out_step + (size_t)(j * BI + i);
+      T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
+      const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
+      T *ob = out + (size_t)nbr[13] * ostep + (size_t)(j * BI + i);
       const int cofs = (j + R) * SJ + (i + RP);  // column (j, i) at kk = 0
       if constexpr (ACC == ACCM_FF) {
         const float2 *ft = reinterpret_cast<const float2 *>(rt);
@@ -439,16 +497,17 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
         }
       }
     }
+    store_adj(nfar);  // group it + 2; read after the next iteration's first barrier
   }
   cp_async_wait<0>();  // no copy may outlive the kernel
 }
 
-template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
-int launch_sweep2(const SweepArgs &a, const Taps &tp, cudaStream_t s) {
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH = false>
+int launch_sweep2(const SweepArgs &a, const Taps &tp, cudaStream_t s, int grid_cap = 0) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
   static_assert(C::SMEM <= 227 * 1024, "tile too large");
   static_assert(BK * BJ * BI <= 8192 && C::TILE <= 16384, "plan entry fields overflow");
-  auto kern = sweep2_kernel<T, BK, BJ, BI, R, FAM, ACC>;
+  auto kern = sweep2_kernel<T, BK, BJ, BI, R, FAM, ACC, BATCH>;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -459,6 +518,7 @@ int launch_sweep2(const SweepArgs &a, const Taps &tp, cudaStream_t s) {
   if (per_sm < 1) return fail(BK_ERR_UNSUPPORTED, "sweep2 kernel does not fit on an SM");
   const long long groups = ((long long)a.nlist + C::NB - 1) / C::NB;
   long long grid = (long long)sms * per_sm;
+  if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
   if (grid > groups) grid = groups;
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, C::NT, C::SMEM, s>>>(a, tp);

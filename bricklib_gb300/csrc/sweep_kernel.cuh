@@ -22,6 +22,16 @@ namespace bk {
 enum Family { FAM_GENERIC = 0, FAM_STAR = 1, FAM_CUBE = 2 };
 enum AccMode { ACCM_NATIVE = 0, ACCM_COMP = 1, ACCM_FF = 2 };
 
+// One domain of a batch (device table entry).
+struct BatchDomain {
+  const unsigned *adj;
+  unsigned nbricks;
+  unsigned stencil;
+  unsigned char *f0, *f1;  // field bases (dat + offset), bytes
+  unsigned long long step_bytes;
+  long long chunks;
+};
+
 struct SweepArgs {
   const unsigned *adj;
   unsigned nbricks;
@@ -35,6 +45,11 @@ struct SweepArgs {
   unsigned nlist;
   int *err;
   Layout L;
+  // batch mode: work items (domain, brick) instead of blist, per-domain fields by parity
+  const BatchDomain *doms;
+  const uint2 *work;
+  unsigned ndom;
+  int parity;
 };
 
 // Coefficients in kernel order; passed by value (kernel parameter constant bank).

@@ -121,9 +121,14 @@ def test_batch_graph_and_plain_bitwise_equal_and_layouts_agree():
         b.close()
         if base is None:
             base = arrs
-        else:
+        elif lay.offsets().tolist() == list(range(lay.size)):
+            # row-major layouts run the same pipelined kernel: bit-identical
             for x, y in zip(base, arrs):
                 np.testing.assert_array_equal(x, y)
+        else:
+            # other folds run the one-shot kernel, which orders cube taps differently
+            for x, y in zip(base, arrs):
+                assert np.abs(x - y).max() <= 1e-6 * np.abs(y).max()
 
 
 def test_domain_alone_equals_domain_in_the_mix():
