@@ -139,6 +139,8 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
     // (measured on GB300: cube125 18.6 vs 12.8, cube27 61 vs 46, star25 17 vs 15 GStencil/s)
     if (plan->acc == ACCM_FF && (plan->fam == FAM_CUBE || plan->r >= 4) && !getenv("BK_SWEEP_PIPELINED"))
       plan->v2 = false;
+    // star stencils on 8x8x8 row-major bricks: the TMA-fed kernel, unless a kernel is forced
+    plan->tma = tma_eligible(*plan, in) && !getenv("BK_SWEEP_ONESHOT") && !getenv("BK_SWEEP_PIPELINED");
   }
   int *err = device_error_word();
   if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
@@ -148,6 +150,7 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
 }
 
 static int dispatch(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
+  if (p.tma) return sweep_dispatch_tma(p, a, tp, s);
   switch (p.dtype) {
     case BK_F64: return sweep_dispatch_f64(p, a, tp, s);
     case BK_F32: return sweep_dispatch_f32(p, a, tp, s);
@@ -169,6 +172,7 @@ int plan_stencil(const bk_stencil *st, const Layout &L, int dtype, int acc, Swee
   if (plan->shape < 0) return fail(BK_ERR_UNSUPPORTED, "brick dims must be 8x8x8, 4x4x4, 16x8x8 or 8x8x32");
   plan->dtype = dtype;
   plan->v2 = false;
+  plan->tma = false;
   if (acc == BK_ACC_NATIVE) plan->acc = ACCM_NATIVE;
   else if (acc == BK_ACC_COMPENSATED && dtype != BK_F64) plan->acc = ACCM_COMP;
   else if (acc == BK_ACC_FLOATFLOAT && dtype == BK_F64) plan->acc = ACCM_FF;

@@ -435,6 +435,7 @@ struct SweepPlan {
   int shape;  // 0: 8x8x8, 1: 4x4x4, 2: 16x8x8, 3: 8x8x32
   bool rm;
   bool v2;    // row-major and aligned: the pipelined kernel applies
+  bool tma;   // star stencil on row-major 8x8x8 bricks, TMA-describable field: the TMA kernel applies
   bool ops;   // pointwise pre / post operations (one-shot kernels only)
   int fam;
   int r;
@@ -446,5 +447,7 @@ struct SweepPlan {
 int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
 int sweep_dispatch_f32(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
 int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
+int sweep_dispatch_tma(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
+bool tma_eligible(const SweepPlan &p, const bk_field *in);
 
 }  // namespace bk

@@ -1,0 +1,85 @@
+// Star stencils on row-major 8x8x8 bricks through the TMA-fed kernel: tensor-map encoding
+// and the instantiations for every storage type.
+#include "sweep3_kernel.cuh"
+
+namespace bk {
+
+// cuTensorMapEncodeTiled, looked up through the runtime so that the library does not link
+// the driver library directly (it loads on machines without a GPU driver).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+bool star_tma_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r, int iw, TmaMaps *maps) {
+  const EncodeTiledFn encode = encode_tiled();
+  if (!encode) return false;
+  const size_t es = dtype_size(dtype);
+  const CUtensorMapDataType ty = dtype == BK_F64   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                 : dtype == BK_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                                   : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  const char *base = reinterpret_cast<const char *>(a.in) + a.in_off * es;
+  if (reinterpret_cast<uintptr_t>(base) % 16 || (a.in_step * es) % 16 || ((size_t)bi * es) % 16) return false;
+  if (a.in_chunks < 1 || a.in_chunks > 0x7FFFFFFFll || a.in_step * es >= (1ull << 40)) return false;
+  // the last brick of the field ends inside the storage: chunks * step covers offset + brick
+  const cuuint64_t dims[4] = {(cuuint64_t)bi, (cuuint64_t)bj, (cuuint64_t)bk, (cuuint64_t)a.in_chunks};
+  const cuuint64_t strides[3] = {(cuuint64_t)(bi * es), (cuuint64_t)(bj * bi * es), (cuuint64_t)(a.in_step * es)};
+  const cuuint32_t boxes[4][4] = {{(cuuint32_t)bi, (cuuint32_t)bj, (cuuint32_t)bk, 1},
+                                  {(cuuint32_t)bi, (cuuint32_t)bj, (cuuint32_t)r, 1},
+                                  {(cuuint32_t)bi, (cuuint32_t)r, (cuuint32_t)bk, 1},
+                                  {(cuuint32_t)iw, (cuuint32_t)bj, (cuuint32_t)bk, 1}};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  for (int m = 0; m < 4; ++m) {
+    const CUresult e = encode(&maps->m[m], ty, 4, const_cast<char *>(base), dims, strides, boxes[m],
+                                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (e != CUDA_SUCCESS) return false;
+  }
+  return true;
+}
+
+#define BK_TMA_CASE(T_, R_, ACC_) \
+  if (p.r == R_ && p.acc == ACC_) return launch_star_tma<T_, 8, 8, 8, R_, ACC_>(a, tp, p.dtype, s);
+#define BK_TMA_RADII(T_, ACC_) BK_TMA_CASE(T_, 1, ACC_) BK_TMA_CASE(T_, 2, ACC_) BK_TMA_CASE(T_, 4, ACC_)
+
+int sweep_dispatch_tma(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
+  if (p.fam != FAM_STAR || p.shape != 0 || !p.rm)
+    return fail(BK_ERR_UNSUPPORTED, "the TMA sweep covers star stencils on row-major 8x8x8 bricks");
+  switch (p.dtype) {
+    case BK_F64:
+      BK_TMA_RADII(double, ACCM_NATIVE)
+      BK_TMA_RADII(double, ACCM_FF)
+      break;
+    case BK_F32:
+      BK_TMA_RADII(float, ACCM_NATIVE)
+      BK_TMA_RADII(float, ACCM_COMP)
+      break;
+    case BK_BF16:
+      BK_TMA_RADII(__nv_bfloat16, ACCM_NATIVE)
+      BK_TMA_RADII(__nv_bfloat16, ACCM_COMP)
+      break;
+  }
+  return fail(BK_ERR_UNSUPPORTED, "no TMA sweep kernel for this storage type / radius / accumulation");
+}
+
+// Whether a sweep with these fields can take the TMA kernel (host-side rules only).
+bool tma_eligible(const SweepPlan &p, const bk_field *in) {
+  if (p.fam != FAM_STAR || p.shape != 0 || !p.rm || p.ops) return false;
+  if (!(p.r == 1 || p.r == 2 || p.r == 4)) return false;
+  const size_t es = dtype_size(in->dtype);
+  const char *base = reinterpret_cast<const char *>(in->dat) + in->offset * es;
+  return reinterpret_cast<uintptr_t>(base) % 16 == 0 && (in->step * es) % 16 == 0 && in->chunks <= 0x7FFFFFFFll;
+}
+
+}  // namespace bk

@@ -22,16 +22,17 @@ GOLD = os.path.join(os.path.dirname(__file__), "golden")
 TOL64 = 1e-12
 
 
-@pytest.fixture(params=["pipelined", "oneshot"])
+@pytest.fixture(params=["default", "pipelined", "oneshot"])
 def kernel(request, monkeypatch):
-    """Row-major aligned sweeps run the pipelined kernel (BK_SWEEP_PIPELINED=1 forces it where
-    the one-shot kernel is preferred); BK_SWEEP_ONESHOT=1 selects the one-shot kernel that
-    also serves every other layout.  Both must pass."""
+    """With no override, star stencils on row-major 8x8x8 bricks run the TMA-fed kernel;
+    BK_SWEEP_PIPELINED=1 forces the cp.async pipelined kernel (also where the one-shot
+    kernel is preferred); BK_SWEEP_ONESHOT=1 selects the one-shot kernel that also serves
+    every other layout.  All must pass."""
+    monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+    monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
     if request.param == "oneshot":
         monkeypatch.setenv("BK_SWEEP_ONESHOT", "1")
-        monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
-    else:
-        monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+    elif request.param == "pipelined":
         monkeypatch.setenv("BK_SWEEP_PIPELINED", "1")
     return request.param
 
@@ -228,6 +229,43 @@ def test_out_of_range_adjacency_is_clamped_and_flagged():
     B.synchronize()
     assert B.error_flags() & 1
     assert B.error_flags() == 0  # reading clears
+
+
+def _sweep_with(env, monkeypatch, dom, st, acc, lst):
+    monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+    monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
+    if env:
+        monkeypatch.setenv(env, "1")
+    # output field = all-ones bytes (NaN in every storage type) before each run
+    raw = dom.storage.host.view(np.uint8).reshape(dom.nbricks, dom.nfields, -1)
+    raw[:, 1, :] = 0xFF
+    dom.upload()
+    B.brickSweep(dom.brick(0), dom.brick(1), lst, st, acc)
+    B.synchronize()
+    assert B.error_flags() == 0
+    dom.download()
+    return dom.storage.host.copy()
+
+
+@pytest.mark.parametrize("dtype,acc", [(BK_F64, BK_ACC_NATIVE), (BK_F64, _abi.BK_ACC_FLOATFLOAT),
+                                       (BK_F32, BK_ACC_NATIVE), (BK_F32, BK_ACC_COMPENSATED),
+                                       (BK_BF16, BK_ACC_NATIVE), (BK_BF16, BK_ACC_COMPENSATED)])
+@pytest.mark.parametrize("name", ["star7", "star13", "star25"])
+def test_tma_star_kernel_equals_pipelined(dtype, acc, name, monkeypatch):
+    """The TMA-fed star kernel sums in the pipelined kernel's order: bit-identical outputs.
+    The domain has enough brick groups for every CTA to cycle through its pipeline stages
+    several times; the second list is odd-length and shorter than one group per CTA."""
+    st = stencils.make(name, 13)
+    dom = GridDomain((128, 256, 256), dtype=dtype)  # 16,384 bricks: 8,192 groups of two
+    arr = stencils.uniform(31, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    short = B.BrickList(np.asarray(dom.interior[:77][::-1], dtype=np.uint32))
+    for lst, nout in ((dom.dev_interior, len(dom.interior)), (short, 77)):
+        got = [_sweep_with(env, monkeypatch, dom, st, acc, lst) for env in (None, "BK_SWEEP_PIPELINED")]
+        np.testing.assert_array_equal(got[0].view(np.uint8), got[1].view(np.uint8))
+        written = got[0].view(np.uint8).reshape(dom.nbricks, dom.nfields, -1)[:, 1, :]
+        assert int(np.count_nonzero((written != 0xFF).any(axis=1))) == nout
 
 
 def test_empty_brick_list_is_a_no_op():
