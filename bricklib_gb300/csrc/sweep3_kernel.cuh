@@ -1,20 +1,29 @@
 // Star-stencil brick sweep fed by the Tensor Memory Accelerator (row-major 8x8x8 bricks).
 //
-// The input field is described to the TMA unit as a 4-D tensor (i, j, k, brick) with the
-// brick's storage step as the outer stride, so every piece of a brick's star
-// neighbourhood is one tiled bulk copy issued by one thread:
-//   centre   box (BI, BJ, BK) of brick adj[b][13]
-//   k faces  box (BI, BJ, R)  of bricks adj[b][4] (last R planes) and adj[b][22] (first R)
-//   j faces  box (BI, R, BK)  of bricks adj[b][10] (last R rows) and adj[b][16] (first R)
-//   i faces  box (IW, BJ, BK) of bricks adj[b][12] (last IW columns) and adj[b][14] (first
-//            IW), IW = R rounded up to whole 16-byte units
+// The input field is described to the TMA unit as a 3-D tensor (j*BI + i, k, brick) with
+// the brick's storage step as the outer stride, so every piece of a brick's star
+// neighbourhood is one tiled bulk copy of whole k-plane rows, issued by one thread:
+//   centre   box (BJ*BI, BK) of brick adj[b][13]
+//   k faces  box (BJ*BI, R)  of bricks adj[b][4] (last R planes) and adj[b][22] (first R)
+//   j faces  box (R*BI, BK)  of bricks adj[b][10] (last R rows of every plane) and
+//            adj[b][16] (first R rows)
+//   i faces  either the whole bricks adj[b][12] and adj[b][14] (an i face is BJ*BK separate
+//            pieces of R elements in memory, which cost as many L2 sectors as the whole brick
+//            but BJ*BK times as many copy requests; whole bricks also give the i taps the
+//            centre's plane stride), or, with NI, box (IW, BJ, BK) of a 4-D view (i, j, k,
+//            brick), IW = R rounded up to whole 16-byte units: less shared memory per brick.
 // Each region lands densely in its own 128-byte aligned slice of a stage buffer; a stage
-// holds NB bricks and completes on one mbarrier (transaction bytes).  Persistent CTAs keep
-// S-1 groups of copies in flight ahead of the group they compute.  Warp 0 is the producer:
-// its lanes 0..7*NB-1 each own one (brick, region) pair, load that region's adjacency entry
-// one group before it is needed and issue its copy.  Every thread computes one (j, i)
-// column of its brick: k taps from registers, i / j taps from shared memory, the region
-// (centre or face) chosen per lane.  Summation order is that of the pipelined kernel.
+// holds NB bricks.  Persistent CTAs, warp-specialised:
+//   * the last warp is the producer: its lanes 0..7*NB-1 each own one (brick, region) pair;
+//     they load the brick list one group and the adjacency entry half a group ahead, and for
+//     each group wait until the consumers have released the stage (mbarrier "empty"), then
+//     post the stage's byte count and issue the copies (mbarrier "full");
+//   * the other warps are consumers: wait for "full", compute, arrive on "empty".  Every
+//     thread computes one (j, i) column of its brick: k taps from registers, i / j taps from
+//     shared memory, the region (centre or face) chosen per lane.
+// No block-wide barrier runs in the loop.  Every wait gives up after about a second, sets a
+// device error flag and stops the CTA (the producer then waits, again bounded, for its
+// copies still in flight).  Summation order is that of the pipelined kernel.
 #pragma once
 
 #include <cuda.h>
@@ -23,30 +32,32 @@
 
 namespace bk {
 
-// The four box shapes over one input field: centre, k face, j face, i face.
+// The box shapes over one input field: whole brick, k face, j face (3-D view) and the
+// narrow i face (4-D view).
 struct TmaMaps {
   CUtensorMap m[4];
 };
 
-template <typename T, int BK, int BJ, int BI, int R>
+constexpr int TMA_MAX_STAGES = 4;
+
+template <typename T, int BK, int BJ, int BI, int R, bool NI>
 struct StarTmaCfg {
   static constexpr int ES = (int)sizeof(T);
-  static constexpr int VE = 16 / ES;                        // elements per 16 bytes
-  static constexpr int IW = cmin(BI, (R + VE - 1) / VE * VE);  // i-face columns fetched
+  static constexpr int IW = NI ? cmin(BI, (R + 16 / ES - 1) / (16 / ES) * (16 / ES)) : BI;  // i-face columns held
   static constexpr int TPB = BJ * BI;
-  static constexpr int NB = cmax(1, cmin(4, 128 / TPB));  // bricks per CTA (7*NB producer lanes)
-  static constexpr int NT = NB * TPB;
+  static constexpr int NB = cmax(1, cmin(4, 128 / TPB));  // bricks per stage (7*NB producer lanes)
+  static constexpr int NC = NB * TPB;                     // consumer threads
+  static constexpr int NT = NC + 32;                      // + the producer warp
   static constexpr int al(int b) { return (b + 127) / 128 * 128; }
   static constexpr int B_C = BK * BJ * BI * ES, B_KF = R * BJ * BI * ES, B_JF = BK * R * BI * ES,
                        B_IF = BK * BJ * IW * ES;
   static constexpr int O_C = 0, O_KL = al(B_C), O_KH = O_KL + al(B_KF), O_JL = O_KH + al(B_KF),
                        O_JH = O_JL + al(B_JF), O_IL = O_JH + al(B_JF), O_IH = O_IL + al(B_IF);
-  static constexpr int BRICK = O_IH + al(B_IF);  // bytes of one brick's stage buffer
+  static constexpr int BRICK = O_IH + al(B_IF);               // bytes of one brick's stage buffer
   static constexpr int TX = B_C + 2 * (B_KF + B_JF + B_IF);  // bytes the copies of one brick deliver
-  static constexpr int S = cmax(2, cmin(4, (48 * 1024) / (NB * BRICK)));  // pipeline stages
-  // after the stage buffers: S mbarriers (8 B each), then S*NB centre brick indices
-  static constexpr int META = 8 * 4 + 4 * 4 * 4;
-  static constexpr int SMEM = 128 + S * NB * BRICK + META;  // + slack to align the base to 128 B
+  // after the stage buffers: full[4], empty[4] mbarriers, centre brick index [4][NB], abort word
+  static constexpr int META = 64 + 4 * TMA_MAX_STAGES * NB + 16;
+  static constexpr int smem(int stages) { return 128 + stages * NB * BRICK + META; }  // + base alignment slack
 };
 
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
@@ -54,6 +65,9 @@ __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
   unsigned done;
@@ -83,6 +97,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
     }
   }
 }
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
 __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, int x, int y, int z, int w,
                                             unsigned bar) {
   asm volatile(
@@ -90,17 +110,34 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
       "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
       : "memory");
 }
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
+// Named barrier over `count` threads with an OR reduction of `pred` (uniform result).
+__device__ __forceinline__ bool bar_red_or(int id, int count, bool pred) {
+  unsigned r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"((unsigned)pred), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
 
-template <typename T, int BK, int BJ, int BI, int R, int ACC>
-__global__ void __launch_bounds__(StarTmaCfg<T, BK, BJ, BI, R>::NT)
-sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp) {
-  typedef StarTmaCfg<T, BK, BJ, BI, R> C;
+template <typename T, int BK, int BJ, int BI, int R, int ACC, bool NI>
+__global__ void __launch_bounds__(StarTmaCfg<T, BK, BJ, BI, R, NI>::NT)
+sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp, const int S) {
+  typedef StarTmaCfg<T, BK, BJ, BI, R, NI> C;
   typedef typename Elem<T>::acc AT;
-  constexpr int NB = C::NB, S = C::S, TPB = C::TPB, IW = C::IW, PK = BJ * BI;
+  constexpr int NB = C::NB, TPB = C::TPB, IW = C::IW, PK = BJ * BI;
   static_assert(7 * NB <= 32, "one producer lane per (brick, region)");
+  static_assert(TPB % 32 == 0, "whole warps per brick");
   static_assert(C::ES == 8 || ACC != ACCM_FF, "float-float needs FP64 storage");
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -108,73 +145,116 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
   const unsigned pad = (128u - (raw & 127u)) & 127u;
   unsigned char *sm = smem_raw + pad;  // 128-byte aligned stage buffers
   const unsigned sbase = raw + pad;
-  const unsigned bar0 = sbase + S * NB * C::BRICK;
-  unsigned *outb = reinterpret_cast<unsigned *>(sm + S * NB * C::BRICK + 32);  // [S][NB]
+  const unsigned full0 = sbase + S * NB * C::BRICK, empty0 = full0 + 8 * TMA_MAX_STAGES;
+  unsigned *outb = reinterpret_cast<unsigned *>(sm + S * NB * C::BRICK + 64);  // [S][NB]
+  volatile int *abort_word = reinterpret_cast<volatile int *>(sm + S * NB * C::BRICK + 64 + 4 * TMA_MAX_STAGES * NB);
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < S; ++s) mbar_init(bar0 + 8 * s, 1);
+    for (int s = 0; s < S; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, C::NC / 32);
+    }
+    *abort_word = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     fence_proxy_async_smem();
   }
   __syncthreads();
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
+  const long long g0 = blockIdx.x, gstep = gridDim.x;
   const int lane = threadIdx.x & 31;
-  const bool prod = threadIdx.x < 32 && lane < 7 * NB;
-  const int pbs = lane / 7, prg = lane - (lane / 7) * 7;  // producer lane: brick slot, region
-  // region prg: 0 centre, 1 k-lo, 2 k-hi, 3 j-lo, 4 j-hi, 5 i-lo, 6 i-hi
-  const int pslot = prg == 0 ? 13 : prg == 1 ? 4 : prg == 2 ? 22 : prg == 3 ? 10 : prg == 4 ? 16 : prg == 5 ? 12 : 14;
-  const int pmap = (prg + 1) >> 1;
-  const int px = prg == 5 ? BI - IW : 0, py = prg == 3 ? BJ - R : 0, pz = prg == 1 ? BK - R : 0;
-  const int poff = prg == 0 ? C::O_C : prg == 1 ? C::O_KL : prg == 2 ? C::O_KH : prg == 3 ? C::O_JL
-                 : prg == 4 ? C::O_JH : prg == 5 ? C::O_IL : C::O_IH;
-  unsigned pv = 0;  // prefetched adjacency entry of this lane's (brick, region)
-  int pact = 0;     // centre lanes: the brick is valid
 
-  auto fetch = [&](long long grp) {
-    pv = 0;
-    pact = 0;
-    if (!prod) return;
-    const long long n = grp * NB + pbs;
-    if (grp >= ngroups || n >= a.nlist) return;
-    const unsigned b = a.blist[n];
-    if (b >= a.nbricks) {
-      if (prg == 0) atomicOr(a.err, FLAG_BOUNDS);
-      return;
-    }
-    unsigned v = a.adj[(size_t)b * 27 + pslot];
-    pact = prg != 0 || ((long long)v < a.out_chunks && (long long)v < a.in_chunks);
-    if ((long long)v >= a.in_chunks || !pact) {
-      atomicOr(a.err, FLAG_BOUNDS);
-      v = 0;
-    }
-    pv = v;
-  };
-  // warp 0: copies of the group whose adjacency is in (pv, pact) into stage st
-  auto issue = [&](int st) {
-    const int act = __shfl_sync(0xFFFFFFFFu, pact, pbs * 7 < 32 ? pbs * 7 : 0);
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, prod && prg == 0 && act);
-    const unsigned bar = bar0 + 8 * st;
-    if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)__popc(m) * (unsigned)C::TX);
-    __syncwarp();
-    if (prod && act)
-      tma_load_4d(sbase + (st * NB + pbs) * C::BRICK + poff, &maps.m[pmap], px, py, pz, (int)pv, bar);
-    if (prod && prg == 0) outb[st * NB + pbs] = act ? pv : 0xFFFFFFFFu;
-  };
-
-  const long long g0 = blockIdx.x;
-  const long long gstep = gridDim.x;
-  if (threadIdx.x < 32) {
-    for (int p = 0; p < S - 1; ++p) {
-      const long long g = g0 + p * gstep;
-      if (g < ngroups) {
-        fetch(g);
-        issue(p);
+  if (threadIdx.x >= C::NC) {
+    // ------------------------------------------------------------------ producer warp
+    const bool prod = lane < 7 * NB;
+    const int pbs = lane / 7, prg = lane - (lane / 7) * 7;  // brick slot, region
+    // region prg: 0 centre, 1 k-lo, 2 k-hi, 3 j-lo, 4 j-hi, 5 i-lo, 6 i-hi
+    const int pslot = prg == 0 ? 13 : prg == 1 ? 4 : prg == 2 ? 22 : prg == 3 ? 10 : prg == 4 ? 16 : prg == 5 ? 12 : 14;
+    const int pmap = prg == 1 || prg == 2 ? 1 : prg == 3 || prg == 4 ? 2 : (NI && prg >= 5 ? 3 : 0);
+    const int px = prg == 3 ? (BJ - R) * BI : (NI && prg == 5 ? BI - IW : 0), py = prg == 1 ? BK - R : 0;
+    const int poff = prg == 0 ? C::O_C : prg == 1 ? C::O_KL : prg == 2 ? C::O_KH : prg == 3 ? C::O_JL
+                   : prg == 4 ? C::O_JH : prg == 5 ? C::O_IL : C::O_IH;
+    // brick-list entry of this lane's brick in group grp (0xFFFFFFFF: none)
+    auto load_b = [&](long long grp) -> unsigned {
+      const long long n = grp * NB + pbs;
+      return (prod && grp < ngroups && n < (long long)a.nlist) ? a.blist[n] : 0xFFFFFFFFu;
+    };
+    auto load_adj = [&](unsigned b) -> unsigned {
+      return (prod && b < a.nbricks) ? a.adj[(size_t)b * 27 + pslot] : 0u;
+    };
+    // lanes 7*NB .. 8*NB-1 prefetch the centre bricks of the group PF iterations ahead into
+    // L2 (no shared memory involved), so that the copies find them there.  They prefetch
+    // brick b of the list itself: adjacency lists hold every brick as its own centre
+    // (slot 13); where one does not, the hint is merely wasted.
+    constexpr int PF = 2;
+    const bool pfl = lane >= 7 * NB && lane < 8 * NB;
+    const int pfs = lane - 7 * NB;
+    auto load_pf = [&](long long grp) -> unsigned {
+      const long long n = grp * NB + pfs;
+      return (pfl && grp < ngroups && n < (long long)a.nlist) ? a.blist[n] : 0xFFFFFFFFu;
+    };
+    unsigned pf = load_pf(g0 + PF * gstep);
+    const char *in_bytes = reinterpret_cast<const char *>(a.in) + a.in_off * C::ES;
+    unsigned bq = load_b(g0);             // group of iteration it
+    unsigned vq = load_adj(bq);
+    unsigned bn = load_b(g0 + gstep);     // group of iteration it+1
+    int it = 0, st = 0;
+    unsigned ph = 0;  // (it / S) & 1
+    for (long long g = g0; g < ngroups; g += gstep, ++it) {
+      // every lane waits (acquire), the warp agrees on the outcome
+      const bool freed = it < S || mbar_wait_bounded(empty0 + 8 * st, ph ^ 1u);
+      if (!__all_sync(0xFFFFFFFFu, freed)) {
+        if (lane == 0) atomicOr(a.err, FLAG_TIMEOUT);
+        *abort_word = 1;
+        break;
       }
+      if (__any_sync(0xFFFFFFFFu, *abort_word != 0)) break;
+      // checks of the entries loaded one iteration ago
+      unsigned v = vq;
+      int act = 0;
+      if (prod && bq != 0xFFFFFFFFu) {
+        if (bq >= a.nbricks) {
+          if (prg == 0) atomicOr(a.err, FLAG_BOUNDS);
+        } else {
+          act = prg != 0 || ((long long)v < a.out_chunks && (long long)v < a.in_chunks);
+          if ((long long)v >= a.in_chunks || !act) {
+            atomicOr(a.err, FLAG_BOUNDS);
+            v = 0;
+          }
+        }
+      }
+      const int bact = __shfl_sync(0xFFFFFFFFu, act, pbs * 7 < 32 ? pbs * 7 : 0);
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, prod && prg == 0 && bact);
+      if (prod && prg == 0) outb[st * NB + pbs] = bact ? v : 0xFFFFFFFFu;
+      __syncwarp();  // the centre indices are written before the phase can complete
+      const unsigned bar = full0 + 8 * st;
+      if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)__popc(m) * (unsigned)C::TX);
+      __syncwarp();
+      if (prod && bact)
+      {
+        if (pmap == 3) tma_load_4d(sbase + (st * NB + pbs) * C::BRICK + poff, &maps.m[3], px, 0, 0, (int)v, bar);
+        else tma_load_3d(sbase + (st * NB + pbs) * C::BRICK + poff, &maps.m[pmap], px, py, (int)v, bar);
+      }
+      // advance the prefetch pipeline
+      bq = bn;
+      vq = load_adj(bn);
+      bn = load_b(g + 2 * gstep);
+      if (++st == S) {
+        st = 0;
+        ph ^= 1u;
+      }
+      if (pfl && (long long)pf < a.in_chunks)
+        prefetch_l2(in_bytes + (size_t)pf * a.in_step * C::ES, (unsigned)(BK * BJ * BI * C::ES));
+      pf = load_pf(g + (PF + 1) * gstep);
     }
-    fetch(g0 + (S - 1) * gstep);
+    // copies of the last S issued iterations may still be in flight after an abort
+    if (lane == 0)
+      for (int q = it - S > 0 ? it - S : 0; q < it; ++q)
+        if (!mbar_wait_bounded(full0 + 8 * (q % S), (unsigned)(q / S) & 1u)) break;
+    return;
   }
 
+  // -------------------------------------------------------------------- consumer warps
   const int bs = threadIdx.x / TPB, lt = threadIdx.x - bs * TPB;
   const int j = lt / BI, i = lt - j * BI;
   // per-lane shared-memory element offsets (from the brick's stage buffer) and k strides
@@ -198,33 +278,28 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     }
   }
 
-  int it = 0, timed_out = 0;
-  for (long long g = g0; g < ngroups; g += gstep, ++it) {
-    // stage (it-1) % S is free again; a wait that gave up anywhere ends the CTA's loop
-    if (__syncthreads_or(timed_out)) break;
-    const int st = it % S;
-    if (threadIdx.x < 32) {
-      const long long gi = g + (S - 1) * gstep;
-      if (gi < ngroups) {
-        issue((it + S - 1) % S);
-        fetch(gi + gstep);
-      }
-    }
-    if (!mbar_wait_bounded(bar0 + 8 * st, (unsigned)(it / S) & 1u)) {
+  int st = 0;
+  unsigned ph = 0;  // phase parity of the stage's current use
+  for (long long g = g0; g < ngroups; g += gstep) {
+    const bool ok = __all_sync(0xFFFFFFFFu, mbar_wait_bounded(full0 + 8 * st, ph));
+    if (!ok) {
       atomicOr(a.err, FLAG_TIMEOUT);
-      timed_out = 1;
+      *abort_word = 1;
     }
     const unsigned ob_idx = outb[st * NB + bs];
-    const bool active = !timed_out && ob_idx != 0xFFFFFFFFu;
+    const bool active = ok && ob_idx != 0xFFFFFFFFu;
     unsigned char *buf = sm + (st * NB + bs) * C::BRICK;
     if constexpr (ACC == ACCM_FF) {
-      // in place, each thread its own elements: raw doubles -> float pairs
+      // in place, each thread its own elements: raw doubles -> float pairs; the brick's
+      // threads then meet on a named barrier that also agrees on stopping
       if (active) {
         double *dv = reinterpret_cast<double *>(buf);
         float2 *fv = reinterpret_cast<float2 *>(buf);
         for (int e = lt; e < C::BRICK / 8; e += TPB) fv[e] = split_f64(dv[e]);
       }
-      __syncthreads();
+      if (bar_red_or(1 + bs, TPB, !ok)) break;
+    } else {
+      if (!ok) break;
     }
     if (active) {
       T *ob = reinterpret_cast<T *>(a.out) + a.out_off + (size_t)ob_idx * a.out_step + (size_t)(j * BI + i);
@@ -304,15 +379,11 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     // the float-float conversion wrote the stage through the generic proxy; order those
     // writes before the copies that refill it
     if constexpr (ACC == ACCM_FF) fence_proxy_async_smem();
-  }
-  // after a wait gave up: wait (bounded) for the copies still in flight into this CTA's
-  // stages (iterations it-1 .. it+S-2 were issued and not consumed)
-  if (__syncthreads_or(timed_out) && threadIdx.x == 0) {
-    for (int q = it - 1; q < it + S - 1; ++q) {
-      if (q < 0) continue;
-      const long long gq = g0 + (long long)q * gstep;
-      if (gq >= ngroups) break;
-      if (!mbar_wait_bounded(bar0 + 8 * (q % S), (unsigned)(q / S) & 1u)) break;
+    __syncwarp();
+    if (lane == 0) mbar_arrive(empty0 + 8 * st);
+    if (++st == S) {
+      st = 0;
+      ph ^= 1u;
     }
   }
 }
@@ -320,20 +391,25 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
 // Host: encode the four box shapes over the input field.  Returns false when the field
 // does not meet the bulk-tensor rules (16-byte aligned base, strides multiple of 16 bytes).
 bool star_tma_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r, int iw, TmaMaps *maps);
+// Pipeline depth: BK_TMA_STAGES (2..4) when set, else `dflt`.
+int tma_stages(int dflt);
 
-template <typename T, int BK, int BJ, int BI, int R, int ACC>
+template <typename T, int BK, int BJ, int BI, int R, int ACC, bool NI>
 int launch_star_tma(const SweepArgs &a, const Taps &tp, int dtype, cudaStream_t s, int grid_cap = 0) {
-  typedef StarTmaCfg<T, BK, BJ, BI, R> C;
-  static_assert(C::SMEM <= 227 * 1024, "stage buffers too large");
+  typedef StarTmaCfg<T, BK, BJ, BI, R, NI> C;
+  // default depth 2: on GB300 more resident CTAs beat deeper pipelines (FP32 star7 at 512^3:
+  // 602 / 490 GStencil/s with 2 / 3 stages)
+  const int S = tma_stages(2);
+  const int smem = C::smem(S);
+  if (smem > 227 * 1024) return fail(BK_ERR_UNSUPPORTED, "TMA sweep stage buffers exceed shared memory");
   TmaMaps maps;
   if (!star_tma_maps(a, dtype, BK, BJ, BI, R, C::IW, &maps)) return fail(BK_ERR_UNSUPPORTED, "field not describable to the TMA unit");
-  auto kern = sweep_star_tma_kernel<T, BK, BJ, BI, R, ACC>;
+  auto kern = sweep_star_tma_kernel<T, BK, BJ, BI, R, ACC, NI>;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess && C::SMEM > 48 * 1024)
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, C::SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, smem);
   if (e != cudaSuccess) return cuda_fail(e, "star TMA sweep launch setup");
   if (per_sm < 1) return fail(BK_ERR_UNSUPPORTED, "star TMA sweep does not fit on an SM");
   const long long groups = ((long long)a.nlist + C::NB - 1) / C::NB;
@@ -341,7 +417,7 @@ int launch_star_tma(const SweepArgs &a, const Taps &tp, int dtype, cudaStream_t 
   if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
   if (grid > groups) grid = groups;
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, C::NT, C::SMEM, s>>>(maps, a, tp);
+  kern<<<(unsigned)grid, C::NT, smem, s>>>(maps, a, tp, S);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "star TMA sweep launch");
   return BK_OK;

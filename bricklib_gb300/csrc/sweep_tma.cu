@@ -1,5 +1,8 @@
 // Star stencils on row-major 8x8x8 bricks through the TMA-fed kernel: tensor-map encoding
 // and the instantiations for every storage type.
+#include <cstdlib>
+#include <cstring>
+
 #include "sweep3_kernel.cuh"
 
 namespace bk {
@@ -30,27 +33,54 @@ bool star_tma_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r,
                                  : dtype == BK_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                                    : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   const char *base = reinterpret_cast<const char *>(a.in) + a.in_off * es;
+  const size_t plane = (size_t)bj * bi;
+  // bulk-tensor rules: 16-byte aligned base and strides, box rows of whole 16-byte units
+  // (the j-face box is r*bi elements wide and starts at (bj - r)*bi)
   if (reinterpret_cast<uintptr_t>(base) % 16 || (a.in_step * es) % 16 || ((size_t)bi * es) % 16) return false;
-  if (a.in_chunks < 1 || a.in_chunks > 0x7FFFFFFFll || a.in_step * es >= (1ull << 40)) return false;
-  // the last brick of the field ends inside the storage: chunks * step covers offset + brick
-  const cuuint64_t dims[4] = {(cuuint64_t)bi, (cuuint64_t)bj, (cuuint64_t)bk, (cuuint64_t)a.in_chunks};
-  const cuuint64_t strides[3] = {(cuuint64_t)(bi * es), (cuuint64_t)(bj * bi * es), (cuuint64_t)(a.in_step * es)};
-  const cuuint32_t boxes[4][4] = {{(cuuint32_t)bi, (cuuint32_t)bj, (cuuint32_t)bk, 1},
-                                  {(cuuint32_t)bi, (cuuint32_t)bj, (cuuint32_t)r, 1},
-                                  {(cuuint32_t)bi, (cuuint32_t)r, (cuuint32_t)bk, 1},
-                                  {(cuuint32_t)iw, (cuuint32_t)bj, (cuuint32_t)bk, 1}};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  for (int m = 0; m < 4; ++m) {
-    const CUresult e = encode(&maps->m[m], ty, 4, const_cast<char *>(base), dims, strides, boxes[m],
-                                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (plane > 256 || a.in_chunks < 1 || a.in_chunks > 0x7FFFFFFFll || a.in_step * es >= (1ull << 40)) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)plane, (cuuint64_t)bk, (cuuint64_t)a.in_chunks};
+  const cuuint64_t strides[2] = {(cuuint64_t)(plane * es), (cuuint64_t)(a.in_step * es)};
+  const cuuint32_t boxes[3][3] = {{(cuuint32_t)plane, (cuuint32_t)bk, 1},
+                                  {(cuuint32_t)plane, (cuuint32_t)r, 1},
+                                  {(cuuint32_t)(r * bi), (cuuint32_t)bk, 1}};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  for (int m = 0; m < 3; ++m) {
+    const CUresult e = encode(&maps->m[m], ty, 3, const_cast<char *>(base), dims, strides, boxes[m], estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (e != CUDA_SUCCESS) return false;
   }
-  return true;
+  // narrow i faces: box (iw, bj, bk) of the 4-D view (i, j, k, brick)
+  const cuuint64_t dims4[4] = {(cuuint64_t)bi, (cuuint64_t)bj, (cuuint64_t)bk, (cuuint64_t)a.in_chunks};
+  const cuuint64_t strides4[3] = {(cuuint64_t)(bi * es), (cuuint64_t)(plane * es), (cuuint64_t)(a.in_step * es)};
+  const cuuint32_t box4[4] = {(cuuint32_t)iw, (cuuint32_t)bj, (cuuint32_t)bk, 1};
+  const cuuint32_t estr4[4] = {1, 1, 1, 1};
+  if (((size_t)iw * es) % 16 || ((size_t)(bi - iw) * es) % 16) return false;
+  return encode(&maps->m[3], ty, 4, const_cast<char *>(base), dims4, strides4, box4, estr4,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-#define BK_TMA_CASE(T_, R_, ACC_) \
-  if (p.r == R_ && p.acc == ACC_) return launch_star_tma<T_, 8, 8, 8, R_, ACC_>(a, tp, p.dtype, s);
+int tma_stages(int dflt) {
+  const char *e = getenv("BK_TMA_STAGES");
+  if (!e) return dflt;
+  const int v = atoi(e);
+  return v >= 2 && v <= TMA_MAX_STAGES ? v : dflt;
+}
+
+// i faces: narrow boxes (less shared memory, more copy requests) or whole bricks; BK_TMA_IFACE
+// = narrow / whole overrides the per-type default
+static bool narrow_iface(int dtype) {
+  const char *e = getenv("BK_TMA_IFACE");
+  if (e && !strcmp(e, "narrow")) return true;
+  if (e && !strcmp(e, "whole")) return false;
+  return dtype == BK_F64;
+}
+
+#define BK_TMA_CASE(T_, R_, ACC_)                                                    \
+  if (p.r == R_ && p.acc == ACC_)                                                   \
+    return narrow_iface(p.dtype) ? launch_star_tma<T_, 8, 8, 8, R_, ACC_, true>(a, tp, p.dtype, s) \
+                                 : launch_star_tma<T_, 8, 8, 8, R_, ACC_, false>(a, tp, p.dtype, s);
 #define BK_TMA_RADII(T_, ACC_) BK_TMA_CASE(T_, 1, ACC_) BK_TMA_CASE(T_, 2, ACC_) BK_TMA_CASE(T_, 4, ACC_)
 
 int sweep_dispatch_tma(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
