@@ -228,7 +228,8 @@ def run_ours(args):
     achieved = points * bytes_pt / (dom_ms * 1e-3) / 1e9
     tr = traffic_table().get(f"{args.dtype}:{args.acc}:{dom}:{n}")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": tr, "kernel": f"sweep_kernel {dom}",
+                "frac": round(achieved / hbm, 4), "traffic": tr,
+                "kernel": f"{B.sweepKernel(b_in, b_out, csts[dom], acc)} {dom}",
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "compute": {"unit": "TFLOP/s", "achieved": round(sts[dom].flops_per_point * points / (dom_ms * 1e-3) / 1e12, 3),
                             "peak": round(fp64_rate.value / 1e12, 3),

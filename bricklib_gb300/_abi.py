@@ -87,6 +87,8 @@ SIGNATURES = {
     "bk_stencil_check": (C.c_int, [_P(bk_stencil), _P(bk_layout), _P(C.c_int), _P(C.c_int)]),
     "bk_sweep": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_field), _vp, C.c_uint,
                            _P(bk_stencil), _P(bk_layout), C.c_int, _vp]),
+    "bk_sweep_kernel": (C.c_int, [_P(bk_field), _P(bk_field), _P(bk_stencil), _P(bk_layout), C.c_int,
+                                  _P(C.c_char_p)]),
     "bk_error_flags": (C.c_int, [_vp, _P(C.c_int)]),
     "bk_ghost_fill": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_layout), _vp]),
     "bk_periodic_plan": (C.c_int, [_vp, _P(C.c_long), _P(C.c_long), _vp, C.c_long, _P(C.c_long)]),

@@ -417,6 +417,15 @@ def brickSweep(bIn: Brick, bOut: Brick, blist: BrickList, st, acc: int = _abi.BK
          C.c_void_p(blist.ptr), blist.n, C.byref(cst), C.byref(bIn.layout.to_c()), acc, stream_ptr(stream))
 
 
+def sweepKernel(bIn: Brick, bOut: Brick, st, acc: int = _abi.BK_ACC_NATIVE) -> str:
+    """Name of the kernel brickSweep would launch for these bricks and stencil (bk_sweep_kernel)."""
+    cst = st if isinstance(st, _abi.bk_stencil) else to_c_stencil(st)
+    name = C.c_char_p()
+    call("bk_sweep_kernel", C.byref(bIn.field()), C.byref(bOut.field()), C.byref(cst),
+         C.byref(bIn.layout.to_c()), acc, C.byref(name))
+    return name.value.decode()
+
+
 class GhostPlan:
     """(dst, src) brick pairs on the device for bk_ghost_fill."""
 

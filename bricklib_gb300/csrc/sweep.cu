@@ -102,15 +102,14 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   return BK_OK;
 }
 
-static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
-                   const unsigned *blist, const bk_stencil *st, const bk_layout *lay, int acc,
-                   SweepPlan *plan, Taps *tp, SweepArgs *a) {
+// Field / stencil / accumulation checks and the kernel choice (everything but the brick lists).
+static int plan_sweep(const bk_field *in, const bk_field *out, const bk_stencil *st, const bk_layout *lay, int acc,
+                      SweepPlan *plan, Taps *tp, Layout *Lout) {
   Layout L;
   int s = check_layout(lay, &L);
   if (s) return s;
   if ((s = check_field(in, L, "in"))) return s;
   if ((s = check_field(out, L, "out"))) return s;
-  if (!adj || !blist || nbricks == 0) return fail(BK_ERR_ARG, "adjacency, brick list and nbricks are required");
   if (in->dtype != out->dtype) return fail(BK_ERR_ARG, "in and out fields must have the same dtype");
   if (in->dat == out->dat && in->step == out->step) {
     const size_t lo = in->offset < out->offset ? in->offset : out->offset;
@@ -142,6 +141,17 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
     // star stencils on 8x8x8 row-major bricks: the TMA-fed kernel, unless a kernel is forced
     plan->tma = tma_eligible(*plan, in) && !getenv("BK_SWEEP_ONESHOT") && !getenv("BK_SWEEP_PIPELINED");
   }
+  *Lout = L;
+  return BK_OK;
+}
+
+static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
+                   const unsigned *blist, const bk_stencil *st, const bk_layout *lay, int acc,
+                   SweepPlan *plan, Taps *tp, SweepArgs *a) {
+  Layout L;
+  int s = plan_sweep(in, out, st, lay, acc, plan, tp, &L);
+  if (s) return s;
+  if (!adj || !blist || nbricks == 0) return fail(BK_ERR_ARG, "adjacency, brick list and nbricks are required");
   int *err = device_error_word();
   if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
   *a = SweepArgs{adj, nbricks, in->dat, in->step, in->offset, in->chunks,
@@ -197,6 +207,17 @@ int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, in
     for (int d = 0; d < 3; ++d) r = abs(st->offsets[t][d]) > r ? abs(st->offsets[t][d]) : r;
   if (radius) *radius = r;
   if (family) *family = p.fam;
+  return BK_OK;
+}
+
+int bk_sweep_kernel(const bk_field *in, const bk_field *out, const bk_stencil *st, const bk_layout *lay, int acc,
+                    const char **name) {
+  if (!name) return fail(BK_ERR_ARG, "name is NULL");
+  SweepPlan plan{};
+  Layout L;
+  int s = plan_sweep(in, out, st, lay, acc, &plan, nullptr, &L);
+  if (s) return s;
+  *name = plan.tma ? "sweep_star_tma_kernel" : plan.v2 ? "sweep2_kernel" : "sweep_kernel";
   return BK_OK;
 }
 

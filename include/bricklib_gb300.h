@@ -151,12 +151,20 @@ int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, in
  *              grid[GB..STRIDEB-GB)^3 of 3axis.cu:167)
  * Neighbour or list indices >= chunks/nbricks are clamped to brick 0 and reported by
  * bk_error_flags() as BK_ERR_BOUNDS; the kernel never reads outside the storage.
- * Two kernels implement it: a pipelined one (row-major layouts, 16-byte aligned input)
- * and a one-shot one (everything).  The environment variables BK_SWEEP_ONESHOT=1 and
- * BK_SWEEP_PIPELINED=1 override the built-in choice (used by the parity tests). */
+ * Three kernels implement it: a TMA-fed one (7/13/25-point stars on row-major 8x8x8
+ * bricks, 16-byte aligned input), a pipelined one (row-major layouts, 16-byte aligned
+ * input) and a one-shot one (everything).  The environment variables BK_SWEEP_ONESHOT=1
+ * and BK_SWEEP_PIPELINED=1 override the built-in choice (used by the parity tests);
+ * BK_TMA_STAGES (2..4) and BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernel. */
 int bk_sweep(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
              const unsigned *blist, unsigned nlist, const bk_stencil *st, const bk_layout *lay,
              int acc, void *stream);
+
+/* Which kernel bk_sweep would launch for these fields, stencil, layout and accumulation
+ * (no launch): *name = "sweep_star_tma_kernel", "sweep2_kernel" or "sweep_kernel" (a
+ * static string).  No reference counterpart: a diagnostic of this implementation. */
+int bk_sweep_kernel(const bk_field *in, const bk_field *out, const bk_stencil *st, const bk_layout *lay,
+                    int acc, const char **name);
 
 /* Reads and clears the device error word set by kernels of this library on the
  * current device (synchronises the stream).  *flags = 0 when all launches were clean;

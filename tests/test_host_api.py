@@ -52,6 +52,38 @@ def test_stencil_families():
     assert f == 0
 
 
+def _kernel_for(name, lay=None, dtype=_abi.BK_F64, acc=_abi.BK_ACC_NATIVE, offset=0, base=1 << 20):
+    """bk_sweep_kernel on host-only field descriptors (the pointer is never dereferenced)."""
+    lay = lay or B.Layout()
+    size = lay.size
+    fin = _abi.bk_field(C.c_void_p(base), 100, 2 * size, offset, dtype)
+    fout = _abi.bk_field(C.c_void_p(base), 100, 2 * size, size if offset == 0 else 0, dtype)
+    out = C.c_char_p()
+    _abi.call("bk_sweep_kernel", C.byref(fin), C.byref(fout), C.byref(B.to_c_stencil(stencils.make(name, 1))),
+              C.byref(lay.to_c()), acc, C.byref(out))
+    return out.value.decode()
+
+
+def test_kernel_choice(monkeypatch):
+    monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+    monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
+    for name in ("star7", "star13", "star25", "heat7"):
+        for dt in (_abi.BK_F64, _abi.BK_F32, _abi.BK_BF16):
+            assert _kernel_for(name, dtype=dt) == "sweep_star_tma_kernel", (name, dt)
+    assert _kernel_for("star7", acc=_abi.BK_ACC_FLOATFLOAT) == "sweep_star_tma_kernel"
+    assert _kernel_for("cube27") == "sweep2_kernel"
+    assert _kernel_for("cube125", dtype=_abi.BK_F32) == "sweep2_kernel"
+    assert _kernel_for("cube27", acc=_abi.BK_ACC_FLOATFLOAT) == "sweep_kernel"
+    assert _kernel_for("cond7") == "sweep_kernel"  # pointwise operations: one-shot kernel only
+    assert _kernel_for("star7", lay=B.Layout((8, 8, 8), (1, 2, 2))) == "sweep_kernel"
+    assert _kernel_for("star7", lay=B.Layout((4, 4, 4), (1, 4, 4))) == "sweep2_kernel"
+    assert _kernel_for("star7", base=(1 << 20) + 8) == "sweep_kernel"  # not 16-byte aligned
+    monkeypatch.setenv("BK_SWEEP_PIPELINED", "1")
+    assert _kernel_for("star7") == "sweep2_kernel"
+    monkeypatch.setenv("BK_SWEEP_ONESHOT", "1")
+    assert _kernel_for("star7") == "sweep_kernel"
+
+
 def test_stencil_errors_are_reported_not_raised_in_c():
     bad = stencils.custom("far", [(0, 0, 9)], [1.0])
     with pytest.raises(_abi.BkError) as e:
