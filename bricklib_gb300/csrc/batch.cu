@@ -176,7 +176,15 @@ int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndo
 #define BK_B2SET(BK_, BJ_, BI_)                                                               \
   BK_B2(BK_, BJ_, BI_, 1, FAM_STAR) BK_B2(BK_, BJ_, BI_, 2, FAM_STAR) BK_B2(BK_, BJ_, BI_, 4, FAM_STAR) \
   BK_B2(BK_, BJ_, BI_, 1, FAM_CUBE) BK_B2(BK_, BJ_, BI_, 2, FAM_CUBE)
-    if (p.shape == 0) { BK_B2SET(8, 8, 8) }
+    if (p.shape == 0) {
+      if constexpr (ACC == ACCM_NATIVE) {  // mirror-symmetric cubes: the pair-sum variant
+        if (p.symij && p.fam == FAM_CUBE && p.r == 1) return launch_sweep2<T, 8, 8, 8, 1, FAM_CUBESYM_IJ, ACC, true>(a, tp, s, grid_cap);
+        if (p.symij && p.fam == FAM_CUBE && p.r == 2) return launch_sweep2<T, 8, 8, 8, 2, FAM_CUBESYM_IJ, ACC, true>(a, tp, s, grid_cap);
+        if (p.sym && p.fam == FAM_CUBE && p.r == 1) return launch_sweep2<T, 8, 8, 8, 1, FAM_CUBESYM, ACC, true>(a, tp, s, grid_cap);
+        if (p.sym && p.fam == FAM_CUBE && p.r == 2) return launch_sweep2<T, 8, 8, 8, 2, FAM_CUBESYM, ACC, true>(a, tp, s, grid_cap);
+      }
+      BK_B2SET(8, 8, 8)
+    }
     if constexpr (ACC == ACCM_NATIVE && sizeof(T) == 4) {
       if (p.shape == 1) { BK_B2SET(4, 4, 4) }
       if (p.shape == 2) { BK_B2SET(16, 8, 8) }

@@ -99,6 +99,33 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   }
   plan->offs = offs;
   plan->toff1 = toff1;
+  // mirror symmetry of a cube in every axis: c(dk,dj,di) == c(|dk|,|dj|,|di|) exactly
+  plan->sym = plan->symij = false;
+  if (fam == FAM_CUBE) {
+    const int w = 2 * r + 1;
+    bool sym = true;
+    for (int t = 0; t < w * w * w && sym; ++t) {
+      const int dk = t / (w * w) - r, dj = (t / w) % w - r, di = t % w - r;
+      const int m = ((abs(dk) + r) * w + (abs(dj) + r)) * w + (abs(di) + r);
+      sym = tp->c[t] == tp->c[m];
+    }
+    if (sym) {
+      plan->sym = true;
+      for (int ak = 0; ak <= r; ++ak)
+        for (int aj = 0; aj <= r; ++aj)
+          for (int ai = 0; ai <= r; ++ai) {
+            const int m = ((ak + r) * w + (aj + r)) * w + (ai + r), q = sym_index(ak, aj, ai, r);
+            tp->c[q] = tp->c[m];
+            tp->cf[q] = tp->cf[m];
+            tp->cl[q] = tp->cl[m];
+          }
+      bool ij = true;
+      for (int ak = 0; ak <= r; ++ak)
+        for (int aj = 0; aj <= r; ++aj)
+          for (int ai = 0; ai <= r; ++ai) ij = ij && tp->c[sym_index(ak, aj, ai, r)] == tp->c[sym_index(ak, ai, aj, r)];
+      plan->symij = ij;
+    }
+  }
   return BK_OK;
 }
 

@@ -438,6 +438,47 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
             }
             store_stream(ob + k * BJ * BI, v);
           }
+        } else if constexpr (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ) {
+          // Mirror-symmetric cube: for every (b, a) = (|dj|, |di|) the column
+          //   q[kk] = sum of x(kk, j +- b, i +- a) over the distinct sign choices
+          // is formed with additions, then
+          //   out(k) += c(0,b,a) q[k] + sum_{c>=1} c(c,b,a) (q[k-c] + q[k+c]).
+          // Per point: 69 instead of 125 floating-point operations for R = 2 (27 multiply-adds,
+          // 42 additions), 18 instead of 27 for R = 1.  With the i <-> j swap symmetry the
+          // columns of (b, a) and (a, b) share their coefficients and are added first: 58.5
+          // operations for R = 2.
+          static_assert(ACC == ACCM_NATIVE, "symmetric cubes: native arithmetic");
+          constexpr bool IJ = FAM == FAM_CUBESYM_IJ;
+          AT acc[BK];
+          // sum of x(kk, j +- b, i +- a) over the distinct sign choices
+          auto ring = [&](const T *c, int b, int a) -> AT {
+            if (a == 0 && b == 0) return to_acc(c[0]);
+            if (b == 0) return to_acc(c[-a]) + to_acc(c[a]);
+            if (a == 0) return to_acc(c[-b * SJ]) + to_acc(c[b * SJ]);
+            return (to_acc(c[-b * SJ - a]) + to_acc(c[-b * SJ + a])) + (to_acc(c[b * SJ - a]) + to_acc(c[b * SJ + a]));
+          };
+#pragma unroll
+          for (int b = 0; b <= R; ++b)
+#pragma unroll
+            for (int a = 0; a <= (IJ ? b : R); ++a) {
+              AT q[BK + 2 * R];
+#pragma unroll
+              for (int kk = 0; kk < BK + 2 * R; ++kk) {
+                const T *c = rt + kk * SK + cofs;
+                q[kk] = (IJ && a != b) ? ring(c, b, a) + ring(c, a, b) : ring(c, b, a);
+              }
+#pragma unroll
+              for (int k = 0; k < BK; ++k) {
+                const AT c0 = coef<AT>(tp, sym_index(0, b, a, R));
+                if (a == 0 && b == 0) acc[k] = c0 * q[k + R];
+                else acc[k] = fma(c0, q[k + R], acc[k]);
+#pragma unroll
+                for (int d = 1; d <= R; ++d)
+                  acc[k] = fma(coef<AT>(tp, sym_index(d, b, a, R)), q[k + R - d] + q[k + R + d], acc[k]);
+              }
+            }
+#pragma unroll
+          for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k]);
         } else if constexpr (FAM == FAM_CUBE) {
           AT acc[BK], comp[BK];
 #pragma unroll

@@ -39,6 +39,13 @@ namespace bk {
 int sweep_dispatch_f32(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
   if (p.v2) {
     if (p.shape == 0) {
+      // mirror-symmetric cubes: pair sums, fewer multiply-adds
+      if (p.sym && p.fam == FAM_CUBE && p.acc == ACCM_NATIVE) {
+        if (p.symij && p.r == 1) return launch_sweep2<float, 8, 8, 8, 1, FAM_CUBESYM_IJ, ACCM_NATIVE>(a, tp, s);
+        if (p.symij && p.r == 2) return launch_sweep2<float, 8, 8, 8, 2, FAM_CUBESYM_IJ, ACCM_NATIVE>(a, tp, s);
+        if (p.r == 1) return launch_sweep2<float, 8, 8, 8, 1, FAM_CUBESYM, ACCM_NATIVE>(a, tp, s);
+        if (p.r == 2) return launch_sweep2<float, 8, 8, 8, 2, FAM_CUBESYM, ACCM_NATIVE>(a, tp, s);
+      }
       BK_SHAPE_SET2(8, 8, 8, ACCM_NATIVE)
       BK_SHAPE_SET2(8, 8, 8, ACCM_COMP)
     } else if (p.shape == 1) {

@@ -19,7 +19,15 @@
 
 namespace bk {
 
-enum Family { FAM_GENERIC = 0, FAM_STAR = 1, FAM_CUBE = 2 };
+// FAM_CUBESYM: a cube whose coefficients are mirror-symmetric in each axis,
+// c(dk, dj, di) = c(|dk|, |dj|, |di|); computed from pair sums (see sweep2_kernel.cuh)
+// FAM_CUBESYM_IJ: in addition c(dk, dj, di) == c(dk, di, dj) (i <-> j swap symmetry)
+enum Family { FAM_GENERIC = 0, FAM_STAR = 1, FAM_CUBE = 2, FAM_CUBESYM = 3, FAM_CUBESYM_IJ = 4 };
+// Taps index of the mirror-symmetric coefficient of (|dk|, |dj|, |di|), radius r: the
+// symmetric table lives after the full cube table (at most 125 entries)
+__host__ __device__ constexpr int sym_index(int ak, int aj, int ai, int r) {
+  return 200 + (ak * (r + 1) + aj) * (r + 1) + ai;
+}
 enum AccMode { ACCM_NATIVE = 0, ACCM_COMP = 1, ACCM_FF = 2 };
 
 // One domain of a batch (device table entry).
@@ -436,6 +444,8 @@ struct SweepPlan {
   bool rm;
   bool v2;    // row-major and aligned: the pipelined kernel applies
   bool tma;   // star stencil on row-major 8x8x8 bricks, TMA-describable field: the TMA kernel applies
+  bool sym;   // cube with mirror-symmetric coefficients (sym_index table filled)
+  bool symij; // ... and symmetric under the i <-> j swap
   bool ops;   // pointwise pre / post operations (one-shot kernels only)
   int fam;
   int r;

@@ -121,12 +121,13 @@ def test_batch_graph_and_plain_bitwise_equal_and_layouts_agree():
         b.close()
         if base is None:
             base = arrs
-        elif lay.offsets().tolist() == list(range(lay.size)):
-            # row-major layouts run the same pipelined kernel: bit-identical
+        elif lay.offsets().tolist() == list(range(lay.size)) and tuple(bdim) == (8, 8, 8):
+            # row-major 8x8x8 layouts run the same pipelined kernel: bit-identical
             for x, y in zip(base, arrs):
                 np.testing.assert_array_equal(x, y)
         else:
-            # other folds run the one-shot kernel, which orders cube taps differently
+            # other folds run the one-shot kernel, which orders cube taps differently, and
+            # only 8x8x8 bricks have the pair-sum path of mirror-symmetric cubes
             for x, y in zip(base, arrs):
                 assert np.abs(x - y).max() <= 1e-6 * np.abs(y).max()
 

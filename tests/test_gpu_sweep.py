@@ -231,6 +231,35 @@ def test_out_of_range_adjacency_is_clamped_and_flagged():
     assert B.error_flags() == 0  # reading clears
 
 
+def _mirror_symmetric_cube(r, seed, ij=False):
+    """A (2r+1)^3 cube whose coefficient depends on (|dk|, |dj|, |di|) only; with `ij` also
+    symmetric under the swap of |dj| and |di|."""
+    taps, _ = stencils.cube_taps(r)
+    per = stencils.uniform01(seed, (r + 1) ** 3).reshape(r + 1, r + 1, r + 1)
+    if ij:
+        per = per + per.transpose(0, 2, 1)
+    c = np.array([per[abs(t[0]), abs(t[1]), abs(t[2])] for t in taps])
+    return stencils.custom(f"symcube{2 * r + 1}", taps, c / c.sum())
+
+
+@pytest.mark.parametrize("ij", [False, True])
+@pytest.mark.parametrize("r", [1, 2])
+@pytest.mark.parametrize("dtype", [BK_F64, BK_F32, BK_BF16])
+def test_mirror_symmetric_cubes_against_oracle(r, dtype, ij, kernel):
+    """Mirror-symmetric cubes take the pair-sum paths of the pipelined kernel (fewer
+    multiply-adds); the result still meets the FP64 / FP32 / BF16 bounds against the oracle."""
+    st = _mirror_symmetric_cube(r, 40 + r, ij)
+    dom, arr, got = device_sweep(32, st, dtype=dtype, seed=17)
+    if dtype == BK_F64:
+        ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+        assert ok, f"max |diff| {md}"
+    elif dtype == BK_F32:
+        assert normwise(got, oracle_array(dom, arr.astype(np.float32).astype(np.float64), st)) <= 1e-5
+    else:
+        arr_b = B.bf16_to_f32(B.f32_to_bf16(arr.astype(np.float32))).astype(np.float64)
+        assert normwise(got, oracle_array(dom, arr_b, st)) <= 2.0 ** -7
+
+
 def _sweep_with(env, monkeypatch, dom, st, acc, lst):
     monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
     monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
