@@ -51,6 +51,11 @@ class bk_batch_domain(C.Structure):
                 ("nlist", C.c_uint), ("pairs", C.c_void_p), ("npairs", C.c_uint), ("stencil", C.c_int)]
 
 
+class bk_decomp_region(C.Structure):
+    _fields_ = [("neighbor", C.c_uint64), ("skin_st", C.c_uint), ("skin_ed", C.c_uint), ("pos", C.c_uint),
+                ("len", C.c_uint), ("first_pad", C.c_uint), ("last_pad", C.c_uint)]
+
+
 class bk_job_desc(C.Structure):
     _fields_ = [("n", C.c_long * 3), ("stencil", C.POINTER(bk_stencil)), ("steps", C.c_int), ("dtype", C.c_int),
                 ("acc", C.c_int), ("input", C.c_void_p), ("output", C.c_void_p)]
@@ -90,6 +95,14 @@ SIGNATURES = {
     "bk_sweep_kernel": (C.c_int, [_P(bk_field), _P(bk_field), _P(bk_stencil), _P(bk_layout), C.c_int,
                                   _P(C.c_char_p)]),
     "bk_error_flags": (C.c_int, [_vp, _P(C.c_int)]),
+    "bk_decomp_create": (C.c_int, [C.c_int, _P(C.c_uint), _P(C.c_uint), C.c_uint, C.c_uint, C.c_size_t, C.c_long,
+                                   _P(C.c_uint64), C.c_uint, _P(_vp)]),
+    "bk_decomp_info": (C.c_int, [_vp, _P(C.c_uint), _P(C.c_size_t), _P(C.c_uint), _P(C.c_uint)]),
+    "bk_decomp_grid": (C.c_int, [_vp, _P(C.c_uint)]),
+    "bk_decomp_adjacency": (C.c_int, [_vp, _P(C.c_uint)]),
+    "bk_decomp_regions": (C.c_int, [_vp, _P(bk_decomp_region), _P(bk_decomp_region), _P(C.c_long)]),
+    "bk_decomp_exchange_links": (C.c_int, [_vp, _vp, C.c_size_t, _P(C.c_uint64)]),
+    "bk_decomp_destroy": (None, [_vp]),
     "bk_ghost_fill": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_layout), _vp]),
     "bk_periodic_plan": (C.c_int, [_vp, _P(C.c_long), _P(C.c_long), _vp, C.c_long, _P(C.c_long)]),
     "bk_region_copy": (C.c_int, [_vp, C.c_uint, _vp]),

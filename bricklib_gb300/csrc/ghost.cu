@@ -21,18 +21,21 @@ ghost_fill_kernel(const unsigned *__restrict__ pairs, unsigned npairs, unsigned 
   }
 }
 
-// strong/main.cu:76-83 cudaCopy: one CTA per {from, to, bytes} link, 8- or 16-byte words.
+// strong/main.cu:76-83 cudaCopy over {from, to, bytes} links.  Every CTA walks every link
+// and copies its share of it (16-byte words where the link allows, else 8-byte words), so
+// both many small links and a few large ones spread over the whole grid.
 __global__ void __launch_bounds__(256) region_copy_kernel(const uint64_t *__restrict__ links, unsigned nlinks) {
-  for (unsigned l = blockIdx.x; l < nlinks; l += gridDim.x) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (uint64_t)gridDim.x * blockDim.x;
+  for (unsigned l = 0; l < nlinks; ++l) {
     const uint64_t from = links[3 * l], to = links[3 * l + 1], bytes = links[3 * l + 2];
     if (((from | to | bytes) & 15) == 0) {
       const uint4 *s = reinterpret_cast<const uint4 *>(from);
       uint4 *d = reinterpret_cast<uint4 *>(to);
-      for (uint64_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) d[w] = s[w];
+      for (uint64_t w = t; w < bytes / 16; w += nt) d[w] = s[w];
     } else {
       const uint64_t *s = reinterpret_cast<const uint64_t *>(from);
       uint64_t *d = reinterpret_cast<uint64_t *>(to);
-      for (uint64_t w = threadIdx.x; w < bytes / 8; w += blockDim.x) d[w] = s[w];
+      for (uint64_t w = t; w < bytes / 8; w += nt) d[w] = s[w];
     }
   }
 }
@@ -77,8 +80,10 @@ int bk_ghost_fill(const unsigned *pairs, unsigned npairs, const bk_field *f, con
 int bk_region_copy(const uint64_t *links, unsigned nlinks, void *stream) {
   if (nlinks == 0) return BK_OK;
   if (!links) return fail(BK_ERR_ARG, "links is NULL");
-  const unsigned grid = nlinks < (1u << 30) ? nlinks : (1u << 30);
-  region_copy_kernel<<<grid, 256, 0, as_stream(stream)>>>(links, nlinks);
+  int dev = 0, sms = 0;
+  BK_CUDA(cudaGetDevice(&dev));
+  BK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  region_copy_kernel<<<(unsigned)sms * 4, 256, 0, as_stream(stream)>>>(links, nlinks);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "region copy launch");
   return BK_OK;

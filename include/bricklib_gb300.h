@@ -187,10 +187,56 @@ int bk_ghost_fill(const unsigned *pairs, unsigned npairs, const bk_field *f, con
 int bk_periodic_plan(const unsigned *grid, const long nb[3], const long gb[3], unsigned *pairs,
                      long cap, long *npairs);
 
-/* Batched contiguous copies inside device memory, one block per link:
- * the reference's RegionLink / cudaCopy (strong/main.cu:60-83).  links: device array of
- * nlinks {from, to, bytes} triples (uint64 each); bytes must be a multiple of 8. */
+/* Batched contiguous copies inside device memory: the reference's RegionLink / cudaCopy
+ * (strong/main.cu:60-83).  links: device array of nlinks {from, to, bytes} triples (uint64
+ * each); bytes must be a multiple of 8.  All CTAs share every link, so a few large links
+ * (the regions of a BrickDecomp exchange) use the whole GPU. */
 int bk_region_copy(const uint64_t *links, unsigned nlinks, void *stream);
+
+/* ------------------------------------------------------------------ BrickDecomp layout */
+
+/* BrickDecomp's layout producer without MPI (include/brick-mpi.h:178-464): the storage
+ * order in which the inner region, each skin region (in skin-list order, page padded) and
+ * each ghost region are contiguous runs of bricks; the grid (position -> brick), the
+ * BrickInfo adjacency and the ghost / skin region records.  On one GPU with periodic
+ * boundaries the exchange (brick-mpi.h:466-499 with one rank) copies skin[i] into ghost[i]
+ * for every record: bk_decomp_exchange_links writes those copies as bk_region_copy links.
+ * Conventions are the reference's: dimension 0 is the contiguous one; a region / neighbour
+ * is a BitSet bit field (bitset.h: side +p of dimension p-1 is bit p, side -p is bit 31+p). */
+typedef struct bk_decomp bk_decomp;
+
+/* g_region of brick-mpi.h:185-193: neighbour set, skin-list range [skin_st, skin_ed), first
+ * brick pos, length len (bricks, including first_pad / last_pad padding bricks). */
+typedef struct bk_decomp_region {
+  uint64_t neighbor;
+  unsigned skin_st, skin_ed, pos, len, first_pad, last_pad;
+} bk_decomp_region;
+
+/* BrickDecomp(dims, depth, numfield) + initialize(skinlist) (brick-mpi.h:298-464).
+ *   dim        1..4
+ *   dims       interior size per dimension in elements, contiguous dimension first
+ *   bdims      brick dims, contiguous dimension first
+ *   depth      ghost depth in elements (a multiple of every brick dim)
+ *   elem_bytes bytes of one element (sizeof(bElem)); with numfield interleaved fields a brick
+ *              occupies bdims product x elem_bytes x numfield bytes
+ *   pagesize   page padding granule in bytes (the reference uses sysconf(_SC_PAGESIZE));
+ *              1 gives the unpadded layout of DECOMP_PAGEUNALIGN builds
+ *   skinlist   nskin regions, e.g. the reference's skin3d_good order */
+int bk_decomp_create(int dim, const unsigned *dims, const unsigned *bdims, unsigned depth, unsigned numfield,
+                     size_t elem_bytes, long pagesize, const uint64_t *skinlist, unsigned nskin, bk_decomp **out);
+/* nbricks (storage chunks, = sep_pos[2]), grid positions (product of dims + 2 x ghost
+ * bricks), number of ghost (= skin) records, sep_pos[3] (inner / skin / ghost ends). */
+int bk_decomp_info(const bk_decomp *d, unsigned *nbricks, size_t *grid_size, unsigned *nregions, unsigned *sep_pos);
+/* grid[position] = brick, position = sum of coordinate x stride, dimension 0 fastest. */
+int bk_decomp_grid(const bk_decomp *d, unsigned *grid);
+/* nbricks x 3^dim adjacency (slot = sum of (offset_d + 1) x 3^d; 0 outside the grid). */
+int bk_decomp_adjacency(const bk_decomp *d, unsigned *adj);
+/* ghost and skin records (nregions each) and the per-skin-list-entry sizes (nskin). */
+int bk_decomp_regions(const bk_decomp *d, bk_decomp_region *ghost, bk_decomp_region *skin, long *skin_size);
+/* The periodic single-GPU exchange of a storage at `dat` with chunk stride step_bytes as
+ * nregions {from, to, bytes} links (host array of 3 x nregions) for bk_region_copy. */
+int bk_decomp_exchange_links(const bk_decomp *d, const void *dat, size_t step_bytes, uint64_t *links);
+void bk_decomp_destroy(bk_decomp *d);
 
 /* ------------------------------------------------------------------ precision form */
 

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "brick.h"
+#include "brick-decomp.h"
 #include "brick-gb300.h"
 #include "brickcompare.h"
 #include "bricksetup.h"
@@ -46,6 +47,75 @@ static std::vector<Tap> cube(int r) {
     for (int j = -r; j <= r; ++j)
       for (int i = -r; i <= r; ++i) t.push_back({k, j, i});
   return t;
+}
+
+// single/mpi.cpp:58-121 on one GPU: a BrickDecomp layout, the reference's adjacency symmetry
+// check, then the periodic exchange + the 7-point sweep against the array kernel on a
+// periodically wrapped array.
+static void decomp_check(std::mt19937_64 &mt) {
+  std::uniform_real_distribution<bElem> u(-1, 1);
+  BrickDecomp<3, 8, 8, 8> bDecomp({N, N, N}, GZ, 2);
+  bDecomp.initialize(skin3d_good);
+  BrickInfo<3> bInfo = bDecomp.getBrickInfo();
+  const long bSize = cal_size<8, 8, 8>::value;
+  auto bStorage = bInfo.allocate(bSize * 2);
+  std::vector<unsigned> grid(STRIDEB * STRIDEB * STRIDEB);
+  for (long k = 0; k < STRIDEB; ++k)
+    for (long j = 0; j < STRIDEB; ++j)
+      for (long i = 0; i < STRIDEB; ++i) grid[(k * STRIDEB + j) * STRIDEB + i] = bDecomp[k][j][i];
+  for (long k = 1; k < STRIDEB - 1; ++k)
+    for (long j = 1; j < STRIDEB - 1; ++j)
+      for (long i = 1; i < STRIDEB - 1; ++i) {
+        const unsigned l = grid[(k * STRIDEB + j) * STRIDEB + i];
+        for (long id = 0; id < 27; ++id)
+          if (bInfo.adj[bInfo.adj[l][id]][26 - id] != l) throw std::runtime_error("decomp: adjacency not symmetric");
+      }
+  // interior values only; the exchange fills the ghost bricks
+  const long size = (long)STRIDE * STRIDE * STRIDE;
+  std::vector<bElem> in(size, 0.0), out(size, 0.0);
+  bElem(*a)[STRIDE][STRIDE] = (bElem(*)[STRIDE][STRIDE])in.data();
+  for (long k = PADDING + GZ; k < PADDING + GZ + N; ++k)
+    for (long j = PADDING + GZ; j < PADDING + GZ + N; ++j)
+      for (long i = PADDING + GZ; i < PADDING + GZ + N; ++i) a[k][j][i] = u(mt);
+  Brick3D bIn(&bInfo, bStorage, 0);
+  copyToBrick<3>({STRIDEG, STRIDEG, STRIDEG}, {PADDING, PADDING, PADDING}, {0, 0, 0}, in.data(), grid.data(), bIn);
+  // the array's periodic wrap (ghost cells <- the opposite interior cells)
+  auto wrap = [](long x) { return PADDING + GZ + ((x - PADDING - GZ) % N + N) % N; };
+  for (long k = PADDING; k < PADDING + STRIDEG; ++k)
+    for (long j = PADDING; j < PADDING + STRIDEG; ++j)
+      for (long i = PADDING; i < PADDING + STRIDEG; ++i) a[k][j][i] = a[wrap(k)][wrap(j)][wrap(i)];
+  bElem(*o)[STRIDE][STRIDE] = (bElem(*)[STRIDE][STRIDE])out.data();
+  const bElem c[7] = {0.4, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1};
+  for (long k = PADDING + GZ; k < PADDING + GZ + N; ++k)
+    for (long j = PADDING + GZ; j < PADDING + GZ + N; ++j)
+      for (long i = PADDING + GZ; i < PADDING + GZ + N; ++i)
+        o[k][j][i] = c[0] * a[k][j][i] + c[1] * a[k][j][i + 1] + c[2] * a[k][j][i - 1] + c[3] * a[k][j + 1][i] +
+                     c[4] * a[k][j - 1][i] + c[5] * a[k + 1][j][i] + c[6] * a[k - 1][j][i];
+  BrickInfo<3> bInfo_dev = movBrickInfo(bInfo, cudaMemcpyHostToDevice);
+  BrickStorage bStorage_dev = movBrickStorage(bStorage, cudaMemcpyHostToDevice);
+  Brick3D bIn_dev(&bInfo_dev, bStorage_dev, 0), bOut_dev(&bInfo_dev, bStorage_dev, bSize);
+  std::vector<unsigned> interior;
+  for (long k = GB; k < STRIDEB - GB; ++k)
+    for (long j = GB; j < STRIDEB - GB; ++j)
+      for (long i = GB; i < STRIDEB - GB; ++i) interior.push_back(grid[(k * STRIDEB + j) * STRIDEB + i]);
+  unsigned *blist_dev = nullptr;
+  gpuCheck(bk_device_malloc((void **)&blist_dev, interior.size() * sizeof(unsigned)));
+  gpuCheck(bk_memcpy(blist_dev, interior.data(), interior.size() * sizeof(unsigned), 0, nullptr));
+  BrickStencil st;
+  st.add(0, 0, 0, c[0]).add(0, 0, 1, c[1]).add(0, 0, -1, c[2]).add(0, 1, 0, c[3]).add(0, -1, 0, c[4]);
+  st.add(1, 0, 0, c[5]).add(-1, 0, 0, c[6]);
+  bDecomp.exchange(bStorage_dev);
+  brickSweep(bIn_dev, bOut_dev, blist_dev, (unsigned)interior.size(), st);
+  int flags = 0;
+  gpuCheck(bk_error_flags(nullptr, &flags));
+  if (flags) throw std::runtime_error("decomp: device error flags");
+  BrickStorage back = movBrickStorage(bStorage_dev, cudaMemcpyDeviceToHost);
+  Brick3D bOut_host(&bInfo, back, bSize);
+  if (!compareBrick<3>({N, N, N}, {PADDING, PADDING, PADDING}, {GZ, GZ, GZ}, out.data(), grid.data(), bOut_host))
+    throw std::runtime_error("decomp: result mismatch!");
+  gpuCheck(bk_device_free(blist_dev));
+  gpuCheck(bk_device_free(bInfo_dev.adj));
+  printf("decomp match\n");
 }
 
 int main() {
@@ -115,6 +185,7 @@ int main() {
   gpuCheck(bk_device_free(bInfo_dev.adj));
   free(grid_ptr);
   free(bInfo.adj);
+  decomp_check(mt);
   printf("result match\n");
   return 0;
 }
