@@ -11,6 +11,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libbrick_gb300.so")
 
 BK_MAX_TAPS = 343
+BK_MAX_TAPS4 = 81
 
 BK_OK, BK_ERR_ARG, BK_ERR_CUDA, BK_ERR_NOMEM, BK_ERR_UNSUPPORTED, BK_ERR_BOUNDS, BK_ERR_BUDGET, \
     BK_ERR_STATE, BK_ERR_TIMEOUT = range(9)
@@ -49,6 +50,14 @@ class bk_batch_domain(C.Structure):
     _fields_ = [("adj", C.c_void_p), ("nbricks", C.c_uint), ("dat", C.c_void_p), ("chunks", C.c_long),
                 ("step", C.c_size_t), ("off0", C.c_size_t), ("off1", C.c_size_t), ("blist", C.c_void_p),
                 ("nlist", C.c_uint), ("pairs", C.c_void_p), ("npairs", C.c_uint), ("stencil", C.c_int)]
+
+
+class bk_layout4(C.Structure):
+    _fields_ = [("bdim", C.c_int * 4), ("fold", C.c_int * 4)]
+
+
+class bk_stencil4(C.Structure):
+    _fields_ = [("npoints", C.c_int), ("offsets", (C.c_int * 4) * BK_MAX_TAPS4), ("coeff", C.c_double * BK_MAX_TAPS4)]
 
 
 class bk_decomp_region(C.Structure):
@@ -95,6 +104,8 @@ SIGNATURES = {
     "bk_sweep_kernel": (C.c_int, [_P(bk_field), _P(bk_field), _P(bk_stencil), _P(bk_layout), C.c_int,
                                   _P(C.c_char_p)]),
     "bk_error_flags": (C.c_int, [_vp, _P(C.c_int)]),
+    "bk_sweep4": (C.c_int, [_vp, C.c_uint, _P(bk_field), _P(bk_field), _vp, C.c_uint, _P(bk_stencil4),
+                            _P(bk_layout4), _vp]),
     "bk_decomp_create": (C.c_int, [C.c_int, _P(C.c_uint), _P(C.c_uint), C.c_uint, C.c_uint, C.c_size_t, C.c_long,
                                    _P(C.c_uint64), C.c_uint, _P(_vp)]),
     "bk_decomp_info": (C.c_int, [_vp, _P(C.c_uint), _P(C.c_size_t), _P(C.c_uint), _P(C.c_uint)]),

@@ -1,0 +1,159 @@
+// Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
+// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  One CTA of 256 threads computes one
+// listed brick at a time: it stages the 81 adjacency entries, gathers the (4+2R)^4
+// neighbourhood into shared memory (converted once to the arithmetic type), and each thread
+// computes one element.  Out-of-range list or adjacency entries are clamped / skipped and
+// raise the device error flag, as in the 3-D kernels.
+#include "bk_common.cuh"
+
+namespace bk {
+
+struct Layout4 {
+  int b[4], f[4];  // (l, k, j, i), outermost first
+  __host__ __device__ __forceinline__ int size() const { return b[0] * b[1] * b[2] * b[3]; }
+  // in-brick offset: folds right-aligned, vector index over the fold blocks, lane inside
+  __host__ __device__ __forceinline__ int offset(int l, int k, int j, int i) const {
+    const int vl = f[0] * f[1] * f[2] * f[3];
+    const int vec = (((l / f[0]) * (b[1] / f[1]) + k / f[1]) * (b[2] / f[2]) + j / f[2]) * (b[3] / f[3]) + i / f[3];
+    const int lane = (((l % f[0]) * f[1] + k % f[1]) * f[2] + j % f[2]) * f[3] + i % f[3];
+    return vec * vl + lane;
+  }
+};
+
+struct Taps4 {
+  int n;
+  int toff[BK_MAX_TAPS4];  // offsets in the (4+2R)^4 tile
+  double c[BK_MAX_TAPS4];
+  float cf[BK_MAX_TAPS4];
+};
+
+template <typename T, typename AT, int R>
+__global__ void __launch_bounds__(256)
+sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__restrict__ in, unsigned long long in_step,
+              long long in_chunks, T *__restrict__ out, unsigned long long out_step, long long out_chunks,
+              const unsigned *__restrict__ blist, unsigned nlist, const Layout4 L, const Taps4 tp, int *err) {
+  constexpr int B = 4, E = B + 2 * R, TILE = E * E * E * E;
+  __shared__ AT tile[TILE];
+  __shared__ unsigned nbr[81];
+  __shared__ unsigned cur;
+  for (unsigned n = blockIdx.x; n < nlist; n += gridDim.x) {
+    if (threadIdx.x == 0) {
+      unsigned b = blist[n];
+      if (b >= nbricks) {
+        atomicOr(err, FLAG_BOUNDS);
+        b = 0xFFFFFFFFu;
+      }
+      cur = b;
+    }
+    __syncthreads();
+    const unsigned b = cur;
+    if (b != 0xFFFFFFFFu) {
+      for (int s = threadIdx.x; s < 81; s += blockDim.x) {
+        unsigned v = adj[(size_t)b * 81 + s];
+        const bool bad = (long long)v >= in_chunks || (s == 40 && (long long)v >= out_chunks);
+        if (bad) {
+          atomicOr(err, FLAG_BOUNDS);
+          v = s == 40 ? 0xFFFFFFFFu : 0u;
+        }
+        nbr[s] = v;
+      }
+    }
+    __syncthreads();
+    if (b != 0xFFFFFFFFu && nbr[40] != 0xFFFFFFFFu) {
+      for (int e = threadIdx.x; e < TILE; e += blockDim.x) {
+        int r = e;
+        const int ii = r % E; r /= E;
+        const int jj = r % E; r /= E;
+        const int kk = r % E;
+        const int ll = r / E;
+        const int ql = ll < R ? -1 : (ll >= R + B ? 1 : 0), qk = kk < R ? -1 : (kk >= R + B ? 1 : 0);
+        const int qj = jj < R ? -1 : (jj >= R + B ? 1 : 0), qi = ii < R ? -1 : (ii >= R + B ? 1 : 0);
+        const unsigned src = nbr[((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1)];
+        const int o = L.offset(ll - R - ql * B, kk - R - qk * B, jj - R - qj * B, ii - R - qi * B);
+        tile[e] = (AT)Elem<T>::load(in + (size_t)src * in_step + o);
+      }
+    }
+    __syncthreads();
+    if (b != 0xFFFFFFFFu && nbr[40] != 0xFFFFFFFFu && threadIdx.x < B * B * B * B) {
+      const int t = threadIdx.x;
+      const int i = t % B, j = (t / B) % B, k = (t / (B * B)) % B, l = t / (B * B * B);
+      const AT *c = tile + (((l + R) * E + (k + R)) * E + (j + R)) * E + (i + R);
+      AT v;
+      if constexpr (sizeof(AT) == 8) {
+        v = tp.c[0] * c[tp.toff[0]];
+        for (int q = 1; q < tp.n; ++q) v = fma(tp.c[q], c[tp.toff[q]], v);
+      } else {
+        v = tp.cf[0] * c[tp.toff[0]];
+        for (int q = 1; q < tp.n; ++q) v = fmaf(tp.cf[q], c[tp.toff[q]], v);
+      }
+      Elem<T>::store(out + (size_t)nbr[40] * out_step + L.offset(l, k, j, i), v);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, typename AT, int R>
+static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
+                   unsigned nlist, const Layout4 &L, const Taps4 &tp, int *err, cudaStream_t s) {
+  long long grid = nlist < (1u << 30) ? nlist : (1u << 30);
+  sweep4_kernel<T, AT, R><<<(unsigned)grid, 256, 0, s>>>(
+      adj, nbricks, reinterpret_cast<const T *>(in->dat) + in->offset, in->step, in->chunks,
+      reinterpret_cast<T *>(out->dat) + out->offset, out->step, out->chunks, blist, nlist, L, tp, err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "sweep4 launch");
+  return BK_OK;
+}
+
+}  // namespace bk
+
+using namespace bk;
+
+extern "C" {
+
+int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
+              unsigned nlist, const bk_stencil4 *st, const bk_layout4 *lay, void *stream) {
+  if (!st || !lay || !in || !out) return fail(BK_ERR_ARG, "stencil, layout and fields are required");
+  Layout4 L;
+  for (int d = 0; d < 4; ++d) {
+    L.b[d] = lay->bdim[d];
+    L.f[d] = lay->fold[d];
+    if (L.b[d] != 4) return fail(BK_ERR_UNSUPPORTED, "4-D sweeps take 4x4x4x4 bricks (weak/main-4d.cpp)");
+    if (L.f[d] <= 0 || L.b[d] % L.f[d]) return fail(BK_ERR_ARG, "fold must divide the brick dims");
+  }
+  if (!in->dat || !out->dat || in->chunks <= 0 || out->chunks <= 0) return fail(BK_ERR_ARG, "fields need storage");
+  if (in->offset + 256 > in->step || out->offset + 256 > out->step)
+    return fail(BK_ERR_ARG, "field: offset + brick size exceeds step");
+  if (in->dtype != out->dtype || (in->dtype != BK_F64 && in->dtype != BK_F32))
+    return fail(BK_ERR_UNSUPPORTED, "4-D sweeps: FP64 or FP32 storage, the same for in and out");
+  if (in->dat == out->dat && in->step == out->step) {
+    const size_t lo = in->offset < out->offset ? in->offset : out->offset;
+    const size_t hi = in->offset < out->offset ? out->offset : in->offset;
+    if (hi - lo < 256) return fail(BK_ERR_ARG, "in and out fields overlap");
+  }
+  if (st->npoints < 1 || st->npoints > BK_MAX_TAPS4) return fail(BK_ERR_ARG, "4-D stencil npoints out of range");
+  int r = 0;
+  for (int t = 0; t < st->npoints; ++t)
+    for (int d = 0; d < 4; ++d) r = abs(st->offsets[t][d]) > r ? abs(st->offsets[t][d]) : r;
+  if (r > 2) return fail(BK_ERR_UNSUPPORTED, "4-D stencils of radius up to 2");
+  if (nlist == 0) return BK_OK;
+  if (!adj || !blist || nbricks == 0) return fail(BK_ERR_ARG, "adjacency, brick list and nbricks are required");
+  const int R = r <= 1 ? 1 : 2, E = 4 + 2 * R;
+  Taps4 tp;
+  tp.n = st->npoints;
+  for (int t = 0; t < tp.n; ++t) {
+    const int *o = st->offsets[t];
+    tp.toff[t] = ((o[0] * E + o[1]) * E + o[2]) * E + o[3];
+    tp.c[t] = st->coeff[t];
+    tp.cf[t] = (float)st->coeff[t];
+  }
+  int *err = device_error_word();
+  if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
+  cudaStream_t s = as_stream(stream);
+  if (in->dtype == BK_F64)
+    return R == 1 ? launch4<double, double, 1>(adj, nbricks, in, out, blist, nlist, L, tp, err, s)
+                  : launch4<double, double, 2>(adj, nbricks, in, out, blist, nlist, L, tp, err, s);
+  return R == 1 ? launch4<float, float, 1>(adj, nbricks, in, out, blist, nlist, L, tp, err, s)
+                : launch4<float, float, 2>(adj, nbricks, in, out, blist, nlist, L, tp, err, s);
+}
+
+}  // extern "C"

@@ -74,12 +74,17 @@ struct layout_of<Brick<Dim<BDims...>, Dim<Folds...>>> {
 template <unsigned dims>
 BrickInfo<dims> movBrickInfo(BrickInfo<dims> &bInfo, cudaMemcpyKind kind) {
   assert(kind == cudaMemcpyHostToDevice || kind == cudaMemcpyDeviceToHost);
-  static_assert(dims == 3, "device adjacency lists are three-dimensional");
   BrickInfo<dims> ret = bInfo;
   const size_t size = (size_t)bInfo.nbricks * static_power<3, dims>::value * sizeof(unsigned);
   if (kind == cudaMemcpyHostToDevice) {
     unsigned *p = nullptr;
-    gpuCheck(bk_info_to_device(&bInfo.adj[0][0], bInfo.nbricks, &p));
+    if (dims == 3) {
+      gpuCheck(bk_info_to_device(&bInfo.adj[0][0], bInfo.nbricks, &p));
+    } else {  // 3^dims entries per brick
+      gpuCheck(bk_device_malloc((void **)&p, size));
+      gpuCheck(bk_memcpy(p, &bInfo.adj[0][0], size, 0, nullptr));
+      gpuCheck(bk_stream_synchronize(nullptr));
+    }
     ret.adj = (typename BrickInfo<dims>::adjlist)p;
   } else {
     ret.adj = (typename BrickInfo<dims>::adjlist)malloc(size);
@@ -154,6 +159,39 @@ inline void brickSweep(BrickT &bIn, BrickT &bOut, const unsigned *blist_dev, uns
   const bk_layout lay = brick_gb300::layout_of<BrickT>::get();
   gpuCheck(bk_sweep(&bIn.bInfo->adj[0][0], bIn.bInfo->nbricks, &in, &out, blist_dev, nlist, &st, &lay, acc,
                     (void *)stream));
+}
+
+/// 4-D tap-list builder: BrickStencil4 st; st.add(dl, dk, dj, di, c) ...
+struct BrickStencil4 : bk_stencil4 {
+  BrickStencil4() : bk_stencil4() {}
+  BrickStencil4 &add(int dl, int dk, int dj, int di, double c) {
+    if (npoints < BK_MAX_TAPS4) {
+      offsets[npoints][0] = dl;
+      offsets[npoints][1] = dk;
+      offsets[npoints][2] = dj;
+      offsets[npoints][3] = di;
+      coeff[npoints] = c;
+      ++npoints;
+    }
+    return *this;
+  }
+};
+
+/// One sweep of a 4-D Brick<Dim<4,4,4,4>, Dim<fold>> (weak/main-4d.cpp) over a device brick list.
+template <typename BrickT>
+inline void brickSweep4(BrickT &bIn, BrickT &bOut, const unsigned *blist_dev, unsigned nlist, const bk_stencil4 &st,
+                        cudaStream_t stream = 0) {
+  static_assert(BrickT::DIMS == 4, "brickSweep4 takes four-dimensional bricks");
+  typedef typename BrickT::BD BD;
+  typedef typename BrickT::FD FD;
+  bk_layout4 lay;
+  for (unsigned d = 0; d < 4; ++d) {
+    lay.bdim[d] = (int)BD::get(d);
+    lay.fold[d] = (int)brick_detail::fold_of<BD, FD>(d);
+  }
+  const bk_field in = brickField(bIn), out = brickField(bOut);
+  gpuCheck(bk_sweep4(&bIn.bInfo->adj[0][0], bIn.bInfo->nbricks, &in, &out, blist_dev, nlist, &st, &lay,
+                     (void *)stream));
 }
 
 template <typename BrickT>

@@ -171,6 +171,31 @@ int bk_sweep_kernel(const bk_field *in, const bk_field *out, const bk_stencil *s
  * bit 0: out-of-range brick index clamped; bit 1: bounded wait timed out. */
 int bk_error_flags(void *stream, int *flags);
 
+/* ------------------------------------------------------------------ 4-D bricks */
+
+/* Four-dimensional bricks (weak/main-4d.cpp: Brick<Dim<4,4,4,4>, Dim<VFOLD>>, the 9-point
+ * star of stencils/mpi9pt.py).  bdim / fold and tap offsets are (l, k, j, i), outermost
+ * first; folds apply to the innermost dimensions as in the 3-D layout.  Adjacency lists hold
+ * 81 entries per brick, slot ((dl+1)*3 + (dk+1))*9 + (dj+1)*3 + (di+1) (init_grid<4>). */
+#define BK_MAX_TAPS4 81
+
+typedef struct bk_layout4 {
+  int bdim[4];
+  int fold[4];
+} bk_layout4;
+
+typedef struct bk_stencil4 {
+  int npoints;
+  int offsets[BK_MAX_TAPS4][4];
+  double coeff[BK_MAX_TAPS4];
+} bk_stencil4;
+
+/* One 4-D sweep over the listed bricks: out = sum c_t * in(l+dl, k+dk, j+dj, i+di).  4x4x4x4
+ * bricks, FP64 or FP32 storage (native arithmetic), radius up to 2.  Same field, list and
+ * error conventions as bk_sweep. */
+int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
+              unsigned nlist, const bk_stencil4 *st, const bk_layout4 *lay, void *stream);
+
 /* ------------------------------------------------------------------ ghost zones */
 
 /* Ghost-zone fill / periodic wrap on the device.  For every (dst, src) pair of brick

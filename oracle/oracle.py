@@ -81,6 +81,9 @@ def ref() -> Optional[C.CDLL]:
         R.ref_init_grid.argtypes = [C.c_long, C.c_long, C.c_long, _u32p, _u32p]
         R.ref_sweep.argtypes = [C.c_int, C.c_long, _f64p, C.c_int, _i32p, _f64p, _f64p, _f64p]
         R.ref_cond.argtypes = [C.c_long, _f64p, _f64p, _f64p, _f64p]
+        R.ref_layout_offsets4.argtypes = [C.c_int, _i64p]
+        R.ref_init_grid4.argtypes = [C.c_long, C.c_long, C.c_long, C.c_long, _u32p, _u32p]
+        R.ref_sweep4.argtypes = [C.c_int, C.c_long, _f64p, C.c_int, _i32p, _f64p, _f64p, _f64p]
         _ref = R
     return _ref
 

@@ -156,6 +156,80 @@ int cond_sweep(long n, const double *in_arr, const double *coeff, double *out_br
   return ok ? 1 : 0;
 }
 
+// ------------------------------------------------------------------ 4-D (weak/main-4d.cpp)
+// Brick<Dim<4,4,4,4>, Dim<VFOLD>> with the folds of main-4d.cpp:33-52 (AVX512 (2,4),
+// AVX2 (2,2), scalar (1)), init_grid<4>, copyToBrick<4> / copyFromBrick<4> / compareBrick<4>
+// and the accessor form of the mpi9pt.py kernel generalised to a runtime 4-D tap list; ghost
+// zone 2*TILE = 8 and array padding 4 as in main-4d.cpp:29-31.
+constexpr long GZ4 = 8, PAD4 = 4;
+
+template <typename Fold>
+void offsets4(long *out) {
+  typedef Brick<Dim<4, 4, 4, 4>, Fold> B;
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<4>(grid_ptr, {1, 1, 1, 1});
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, B::BRICKSIZE);
+  B br(&bInfo, bStorage, 0);
+  for (unsigned l = 0; l < 4; ++l)
+    for (unsigned k = 0; k < 4; ++k)
+      for (unsigned j = 0; j < 4; ++j)
+        for (unsigned i = 0; i < 4; ++i) out[((l * 4 + k) * 4 + j) * 4 + i] = (long)(&br[0][l][k][j][i] - br.dat);
+  free(grid_ptr);
+  free(bInfo.adj);
+}
+
+template <typename Fold>
+int sweep4(long n, const double *in_arr, int npts, const int *offs, const double *coeff, double *out_brick,
+           double *out_arr) {
+  typedef Brick<Dim<4, 4, 4, 4>, Fold> B;
+  const long S = n + 2 * (GZ4 + PAD4), SG = n + 2 * GZ4, gb = SG / 4;
+  const long sz = S * S * S * S;
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<4>(grid_ptr, {gb, gb, gb, gb});
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, B::BRICKSIZE * 2);
+  B bIn(&bInfo, bStorage, 0), bOut(&bInfo, bStorage, B::BRICKSIZE);
+  std::memset(bStorage.dat.get(), 0, sizeof(bElem) * bStorage.chunks * bStorage.step);
+  bElem *in_ptr = (bElem *)aligned_alloc(ALIGN, sizeof(bElem) * sz);
+  std::memcpy(in_ptr, in_arr, sizeof(bElem) * sz);
+  copyToBrick<4>({SG, SG, SG, SG}, {PAD4, PAD4, PAD4, PAD4}, {0, 0, 0, 0}, in_ptr, grid_ptr, bIn);
+  auto at = [&](long l, long k, long j, long i) { return in_ptr[((l * S + k) * S + j) * S + i]; };
+  std::memset(out_arr, 0, sizeof(bElem) * sz);
+  for (long l = PAD4; l < PAD4 + SG; ++l)
+    for (long k = PAD4; k < PAD4 + SG; ++k)
+      for (long j = PAD4; j < PAD4 + SG; ++j)
+        for (long i = PAD4; i < PAD4 + SG; ++i) {
+          bElem v = coeff[0] * at(l + offs[0], k + offs[1], j + offs[2], i + offs[3]);
+          for (int t = 1; t < npts; ++t)
+            v = v + coeff[t] * at(l + offs[4 * t], k + offs[4 * t + 1], j + offs[4 * t + 2], i + offs[4 * t + 3]);
+          out_arr[((l * S + k) * S + j) * S + i] = v;
+        }
+  auto grid = (unsigned(*)[gb][gb][gb])grid_ptr;
+  const long g = GZ4 / 4;
+  for (long tl = g; tl < gb - g; ++tl)
+    for (long tk = g; tk < gb - g; ++tk)
+      for (long tj = g; tj < gb - g; ++tj)
+        for (long ti = g; ti < gb - g; ++ti) {
+          unsigned b = grid[tl][tk][tj][ti];
+          for (long l = 0; l < 4; ++l)
+            for (long k = 0; k < 4; ++k)
+              for (long j = 0; j < 4; ++j)
+                for (long i = 0; i < 4; ++i) {
+                  bElem v = coeff[0] * bIn[b][l + offs[0]][k + offs[1]][j + offs[2]][i + offs[3]];
+                  for (int t = 1; t < npts; ++t)
+                    v = v + coeff[t] * bIn[b][l + offs[4 * t]][k + offs[4 * t + 1]][j + offs[4 * t + 2]]
+                                          [i + offs[4 * t + 3]];
+                  bOut[b][l][k][j][i] = v;
+                }
+        }
+  bool ok = compareBrick<4>({n, n, n, n}, {PAD4, PAD4, PAD4, PAD4}, {GZ4, GZ4, GZ4, GZ4}, out_arr, grid_ptr, bOut);
+  std::memset(out_brick, 0, sizeof(bElem) * sz);
+  copyFromBrick<4>({n, n, n, n}, {PAD4, PAD4, PAD4, PAD4}, {GZ4, GZ4, GZ4, GZ4}, out_brick, grid_ptr, bOut);
+  free(in_ptr);
+  free(grid_ptr);
+  free(bInfo.adj);
+  return ok ? 1 : 0;
+}
+
 typedef Lay<8, 8, 8, Dim<4, 8>> L0;     // CUDA fold (stencils/cudavfold.h:9)
 typedef Lay<8, 8, 8, Dim<8>> L1;        // AVX-512 fold (stencils/cpuvfold.h:12-13)
 typedef Lay<8, 8, 8, Dim<2, 2>> L2;     // docs/usingbricks.md example fold
@@ -201,6 +275,36 @@ int ref_sweep(int layout, long n, const double *in_arr, int npts, const int *off
     case 0: return sweep<L0>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
     case 1: return sweep<L1>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
     case 4: return sweep<L4>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
+  }
+  return -1;
+}
+
+/* 4-D: fold ids 0 (2,4)  1 (2,2)  2 (1) of Brick<Dim<4,4,4,4>, Dim<fold>>; out[256] in (l,k,j,i). */
+int ref_layout_offsets4(int fold, long *out) {
+  switch (fold) {
+    case 0: offsets4<Dim<2, 4>>(out); return 0;
+    case 1: offsets4<Dim<2, 2>>(out); return 0;
+    case 2: offsets4<Dim<1>>(out); return 0;
+  }
+  return -1;
+}
+
+int ref_init_grid4(long gl, long gk, long gj, long gi, unsigned *grid, unsigned *adj) {
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<4>(grid_ptr, {gi, gj, gk, gl});
+  std::memcpy(grid, grid_ptr, sizeof(unsigned) * gl * gk * gj * gi);
+  std::memcpy(adj, bInfo.adj, sizeof(unsigned) * 81 * bInfo.nbricks);
+  free(grid_ptr);
+  free(bInfo.adj);
+  return 0;
+}
+
+/* One 4-D sweep on an n^4 interior (ghost 8, padding 4): arrays (n+24)^4, taps (dl,dk,dj,di). */
+int ref_sweep4(int fold, long n, const double *in_arr, int npts, const int *offs, const double *coeff,
+               double *out_brick, double *out_arr) {
+  switch (fold) {
+    case 0: return sweep4<Dim<2, 4>>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
+    case 2: return sweep4<Dim<1>>(n, in_arr, npts, offs, coeff, out_brick, out_arr);
   }
   return -1;
 }

@@ -118,6 +118,60 @@ static void decomp_check(std::mt19937_64 &mt) {
   printf("decomp match\n");
 }
 
+// weak/main-4d.cpp's brick path on one GPU: Brick<Dim<4,4,4,4>, Dim<2,4>>, init_grid<4>,
+// copyToBrick<4>, the 9-point star of stencils/mpi9pt.py through brickSweep4, compareBrick<4>
+// against the array kernel (ghost 8, padding 4).
+static void four_d_check(std::mt19937_64 &mt) {
+  typedef Brick<Dim<4, 4, 4, 4>, Dim<2, 4>> Brick4D;
+  const long n4 = 16, gz = 8, pad = 4, S = n4 + 2 * (gz + pad), SG = n4 + 2 * gz, gb = SG / 4;
+  std::uniform_real_distribution<bElem> u(-1, 1);
+  unsigned *grid_ptr;
+  auto bInfo = init_grid<4>(grid_ptr, {gb, gb, gb, gb});
+  auto bStorage = BrickStorage::allocate(bInfo.nbricks, 512);
+  Brick4D bIn(&bInfo, bStorage, 0);
+  std::vector<bElem> in(S * S * S * S), out(S * S * S * S, 0.0);
+  for (auto &x : in) x = u(mt);
+  copyToBrick<4>({SG, SG, SG, SG}, {pad, pad, pad, pad}, {0, 0, 0, 0}, in.data(), grid_ptr, bIn);
+  auto at = [&](long l, long k, long j, long i) { return in[((l * S + k) * S + j) * S + i]; };
+  const bElem alpha = 0.2, beta = 0.1;
+  for (long l = pad + gz; l < pad + gz + n4; ++l)
+    for (long k = pad + gz; k < pad + gz + n4; ++k)
+      for (long j = pad + gz; j < pad + gz + n4; ++j)
+        for (long i = pad + gz; i < pad + gz + n4; ++i)
+          out[((l * S + k) * S + j) * S + i] =
+              alpha * at(l, k, j, i) + beta * at(l, k, j, i + 1) + beta * at(l, k, j, i - 1) + beta * at(l, k, j + 1, i) +
+              beta * at(l, k, j - 1, i) + beta * at(l, k + 1, j, i) + beta * at(l, k - 1, j, i) +
+              beta * at(l + 1, k, j, i) + beta * at(l - 1, k, j, i);
+  std::vector<unsigned> interior;
+  const long g = gz / 4;
+  for (long tl = g; tl < gb - g; ++tl)
+    for (long tk = g; tk < gb - g; ++tk)
+      for (long tj = g; tj < gb - g; ++tj)
+        for (long ti = g; ti < gb - g; ++ti) interior.push_back(grid_ptr[((tl * gb + tk) * gb + tj) * gb + ti]);
+  unsigned *blist_dev = nullptr;
+  gpuCheck(bk_device_malloc((void **)&blist_dev, interior.size() * sizeof(unsigned)));
+  gpuCheck(bk_memcpy(blist_dev, interior.data(), interior.size() * sizeof(unsigned), 0, nullptr));
+  BrickInfo<4> bInfo_dev = movBrickInfo(bInfo, cudaMemcpyHostToDevice);
+  BrickStorage bStorage_dev = movBrickStorage(bStorage, cudaMemcpyHostToDevice);
+  Brick4D bIn_dev(&bInfo_dev, bStorage_dev, 0), bOut_dev(&bInfo_dev, bStorage_dev, 256);
+  BrickStencil4 st;
+  st.add(0, 0, 0, 0, alpha).add(0, 0, 0, 1, beta).add(0, 0, 0, -1, beta).add(0, 0, 1, 0, beta).add(0, 0, -1, 0, beta);
+  st.add(0, 1, 0, 0, beta).add(0, -1, 0, 0, beta).add(1, 0, 0, 0, beta).add(-1, 0, 0, 0, beta);
+  brickSweep4(bIn_dev, bOut_dev, blist_dev, (unsigned)interior.size(), st);
+  int flags = 0;
+  gpuCheck(bk_error_flags(nullptr, &flags));
+  if (flags) throw std::runtime_error("4-D: device error flags");
+  BrickStorage back = movBrickStorage(bStorage_dev, cudaMemcpyDeviceToHost);
+  Brick4D bOut_host(&bInfo, back, 256);
+  if (!compareBrick<4>({n4, n4, n4, n4}, {pad, pad, pad, pad}, {gz, gz, gz, gz}, out.data(), grid_ptr, bOut_host))
+    throw std::runtime_error("4-D: result mismatch!");
+  gpuCheck(bk_device_free(blist_dev));
+  gpuCheck(bk_device_free(bInfo_dev.adj));
+  free(grid_ptr);
+  free(bInfo.adj);
+  printf("d4pt9 match\n");
+}
+
 int main() {
   std::mt19937_64 mt(20261203);
   std::uniform_real_distribution<bElem> u(-1, 1);
@@ -186,6 +240,7 @@ int main() {
   free(grid_ptr);
   free(bInfo.adj);
   decomp_check(mt);
+  four_d_check(mt);
   printf("result match\n");
   return 0;
 }

@@ -8,6 +8,12 @@ Fixtures written:
   layouts.npz       in-brick element offsets computed by the reference accessor
                     (include/brick.h:213-327) for seven brick-dims / vector-fold pairs
   init_grid.npz     grid and adjacency of init_grid<3> (include/bricksetup.h:73-90) on 5x4x3
+  layouts4.npz      4-D in-brick offsets of Brick<Dim<4,4,4,4>, Dim<fold>> for the folds of
+                    weak/main-4d.cpp:33-52: (2,4), (2,2), (1)
+  init_grid4.npz    grid and adjacency of init_grid<4> on 5x4x3x2
+  sweep4_<name>.npz one 4-D sweep on an 8^4 interior (ghost 8, padding 4, weak/main-4d.cpp):
+                    mpi9pt (stencils/mpi9pt.py, alpha 0.2 / beta 0.1) with fold (2,4) and fold (1),
+                    and a 9-point star with seeded coefficients; input uniform[-1,1) seed 1234
   sweep_<shape>.npz one sweep on a 16^3 interior (sweep_cond7: the reference's cond kernel,
                     |sum coeff * max(x, 0)|, stencils/3axis.cpp:94-163) (+8 ghost, +8 padding) through
                     copyToBrick -> accessor brick kernel -> compareBrick -> copyFromBrick,
@@ -93,6 +99,38 @@ def main():
              ref_match=ok, n=N, seed_in=SEED_IN, seed_coeff=SEED_COEFF, layout=0,
              offsets=st.offsets(), coeff=st.coeff, input_sum=inp.sum(), pre_op=1, post_op=2)
     print(f"{'cond7':22s} compareBrick={ok} max|brick-array|={np.max(np.abs(ob - oa)):.3e}")
+
+    # ---------------------------------------------------------------- 4-D
+    lay4 = {}
+    for fid, fold in ((0, (2, 4)), (1, (2, 2)), (2, (1,))):
+        out = np.zeros(256, dtype=np.int64)
+        assert R.ref_layout_offsets4(fid, out) == 0
+        lay4[f"offsets_{fid}"] = out
+        lay4[f"fold_{fid}"] = np.asarray(fold)
+    np.savez(os.path.join(OUT, "layouts4.npz"), **lay4)
+    dl, dk, dj, di = 2, 3, 4, 5
+    grid = np.zeros(dl * dk * dj * di, dtype=np.uint32)
+    adj = np.zeros(dl * dk * dj * di * 81, dtype=np.uint32)
+    R.ref_init_grid4(dl, dk, dj, di, grid, adj)
+    np.savez(os.path.join(OUT, "init_grid4.npz"), grid=grid, adj=adj, dims=np.asarray([dl, dk, dj, di]))
+    n4 = 8
+    S4 = n4 + 24
+    inp4 = stencils.uniform(SEED_IN, S4 ** 4)
+    taps9 = [(0, 0, 0, 0), (0, 0, 0, 1), (0, 0, 0, -1), (0, 0, 1, 0), (0, 0, -1, 0), (0, 1, 0, 0), (0, -1, 0, 0),
+             (1, 0, 0, 0), (-1, 0, 0, 0)]  # mpi9pt.py order, (dl, dk, dj, di)
+    cases4 = [("mpi9pt", 0, np.array([0.2] + [0.1] * 8)), ("mpi9pt_fold1", 2, np.array([0.2] + [0.1] * 8)),
+              ("star9", 0, stencils.uniform01(SEED_COEFF, 9))]
+    for name, fid, c9 in cases4:
+        offs = np.asarray(taps9, dtype=np.int32).reshape(-1)
+        ob = np.zeros(S4 ** 4)
+        oa = np.zeros(S4 ** 4)
+        ok = R.ref_sweep4(fid, n4, inp4, 9, offs, c9, ob, oa)
+        sl = (slice(12, 12 + n4),) * 4
+        ob = ob.reshape((S4,) * 4)[sl].copy()
+        oa = oa.reshape((S4,) * 4)[sl].copy()
+        np.savez(os.path.join(OUT, f"sweep4_{name}.npz"), out=ob, arr_maxdiff=np.max(np.abs(ob - oa)), ref_match=ok,
+                 n=n4, seed_in=SEED_IN, fold=fid, offsets=np.asarray(taps9), coeff=c9)
+        print(f"{'4d ' + name:22s} compareBrick={ok} max|brick-array|={np.max(np.abs(ob - oa)):.3e}")
 
 
 if __name__ == "__main__":

@@ -18,6 +18,16 @@ def test_loop_script_lowers_to_star13():
     np.testing.assert_array_equal(st.coeff, np.array([0.4, 0.07, 0.03])[cls])
 
 
+def test_four_dimensional_script_lowers_to_the_4d_star():
+    """A 4-D script lowers to (dl, dk, dj, di) taps: the tap set and weights of
+    stencils/mpi9pt.py (bk_sweep4 takes the list as is)."""
+    from bricklib_gb300 import bricks4
+    st = dsl.load_stencil(os.path.join(HERE, "golden", "dsl", "star9_4d_loops.py"), {"A": 0.2, "B": 0.1})
+    want = bricks4.mpi9pt()
+    assert sorted(zip(st.taps, st.coeff)) == sorted(zip(want.taps, want.coeff))
+    assert bricks4.to_c_stencil4(st).npoints == 9
+
+
 def test_nonlinear_and_missing_constants_are_reported(tmp_path):
     p = tmp_path / "bad.py"
     p.write_text("from st.expr import Index\nfrom st.grid import Grid\ni,j,k=Index(0),Index(1),Index(2)\n"

@@ -16,5 +16,5 @@ def test_cpp_single_node_driver():
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "result match" in r.stdout
-    for name in ("d3pt7", "d3pt13", "d3pt25", "d3pt27", "d3pt125", "decomp"):
+    for name in ("d3pt7", "d3pt13", "d3pt25", "d3pt27", "d3pt125", "decomp", "d4pt9"):
         assert f"{name} match" in r.stdout
