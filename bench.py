@@ -227,13 +227,19 @@ def run_ours(args):
     dom_ms = per_shape_ms[dom]
     achieved = points * bytes_pt / (dom_ms * 1e-3) / 1e9
     tr = traffic_table().get(f"{args.dtype}:{args.acc}:{dom}:{n}")
+    instr = fp_instructions_per_point(sts[dom], acc)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": tr,
                 "kernel": f"{B.sweepKernel(b_in, b_out, csts[dom], acc)} {dom}",
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "compute": {"unit": "TFLOP/s", "achieved": round(sts[dom].flops_per_point * points / (dom_ms * 1e-3) / 1e12, 3),
                             "peak": round(fp64_rate.value / 1e12, 3),
-                            "peak_source": f"measured {'FP64' if dtype == _abi.BK_F64 else 'FP32'} FMA rate (bk_measure_fma_rate)"}}
+                            "peak_source": f"measured {'FP64' if dtype == _abi.BK_F64 else 'FP32'} FMA rate (bk_measure_fma_rate)",
+                            "fp_instructions_per_point": instr,
+                            "pipe_frac": round(points / (dom_ms * 1e-3) * instr / (fp64_rate.value / 2), 4),
+                            "note": "achieved counts 2 x taps flop per point; pipe_frac counts the floating-point "
+                                    "instructions the kernel executes per point (mirror-symmetric cubes run on "
+                                    "pair sums) against the measured FMA instruction rate"}}
 
     # the other FP64 arithmetic mode on the same data: per-stencil rate and its normwise
     # error against the first mode's output
@@ -266,28 +272,63 @@ def run_ours(args):
         tot = sum(v["ms"] for v in alt["per_stencil"].values())
         alt["value"] = round(len(shapes) * points / (tot * 1e-3) / 1e9, 3)
 
-    # end to end through the public API: pinned host input -> device, sweeps, results -> host
+    # end to end through the public API: pinned host input -> device (copy), sweeps whose output
+    # field is page-locked host memory (bk_host_malloc, mapped): each result is stored into host
+    # memory by the sweep itself, over NVLink-C2C, with no separate device-to-host copy.  Two
+    # device input buffers: the input of step t+1 is copied on a second stream while step t
+    # sweeps (the link carries the copy and the results in opposite directions).
     e2e = None
     if not args.no_e2e:
         nbytes = nbricks * bsize * esize
-        h_in, h_out = B.PinnedBuffer(nbytes), B.PinnedBuffer(nbytes)
+        h_in = B.PinnedBuffer(nbytes)
+        s_in2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
+        ins = [B.Brick(dinfo, s_in, 0, lay), B.Brick(dinfo, s_in2, 0, lay)]
+        s_hout = B.BrickStorage.allocate_pinned(nbricks, bsize, dtype)
+        s_hout.host[:] = 0
+        b_hout = B.Brick(dinfo, s_hout, 0, lay)
         B.memcpy(h_in.ptr, s_in.ptr, nbytes, 1, sp)
         torch.cuda.synchronize()
+        cstream = torch.cuda.Stream()
+        arrived = [torch.cuda.Event(), torch.cuda.Event()]
+        consumed = [torch.cuda.Event(), torch.cuda.Event()]
         Ke = max(1, min(K, 5))
+
+        def h2d(buf):
+            with torch.cuda.stream(cstream):
+                cstream.wait_event(consumed[buf])
+                B.memcpy(ins[buf].bStorage.ptr, h_in.ptr, nbytes, 0, cstream.cuda_stream)
+                arrived[buf].record(cstream)
+
+        for q in range(2):
+            consumed[q].record(stream)
+        h2d(0)
         for it in range(Ke + 1):
+            cur = it % 2
             if it == 1:
                 torch.cuda.synchronize()
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            B.memcpy(s_in.ptr, h_in.ptr, nbytes, 0, sp)
+            if it < Ke:
+                h2d(1 - cur)  # the next step's input, while this step sweeps
+            stream.wait_event(arrived[cur])
             for name in shapes:
-                sweep(name)
-                B.memcpy(h_out.ptr, s_out.ptr, nbytes, 1, sp)
+                B.brickSweep(ins[cur], b_hout, blist, csts[name], acc, stream=sp)
+            consumed[cur].record(stream)
         e1.record(stream)
         torch.cuda.synchronize()
         e_ms = e0.elapsed_time(e1) / Ke
+        # the host copy of the last result equals the device sweep's
+        sweep(shapes[-1])
+        dev_out = np.empty(nbricks * bsize, dtype=B.NP_DTYPE[dtype])
+        B.memcpy(dev_out.ctypes.data, s_out.ptr, nbytes, 1, sp)
+        B.synchronize(sp)
+        if not np.array_equal(dev_out.view(np.uint8), s_hout.host.view(np.uint8)):
+            raise RuntimeError("sweep into host memory differs from the device sweep")
         e2e = {"value": round(ws * len(shapes) * points / (e_ms * 1e-3) / 1e9, 3), "unit": "GStencil/s",
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3)}
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3),
+               "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a "
+                       "copy stream, overlapped with the previous step's sweeps; results: stored by each sweep "
+                       "into mapped page-locked host memory over NVLink-C2C"}
 
     # CPU baseline: the oracle's OpenMP brick sweep on a sample of the same bricks,
     # also used as a spot check of the GPU output on those bricks
@@ -312,6 +353,23 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def fp_instructions_per_point(st, acc) -> float:
+    """Floating-point instructions per point of the kernel that runs `st` (native arithmetic on
+    8x8x8 row-major bricks): a multiply-add per tap, except mirror-symmetric cubes, which the
+    pipelined kernel evaluates from pair sums (sweep2_kernel.cuh, FAM_CUBESYM)."""
+    from bricklib_gb300 import _abi
+    taps = [tuple(t) for t in st.taps]
+    r = st.radius
+    cube = len(taps) == (2 * r + 1) ** 3 and len(set(taps)) == len(taps) and r in (1, 2)
+    if not cube or acc != _abi.BK_ACC_NATIVE:
+        return float(len(taps))
+    c = {t: v for t, v in zip(taps, st.coeff)}
+    if any(c[t] != c[tuple(abs(a) for a in t)] for t in taps):
+        return float(len(taps))
+    ij = all(c[(k, j, i)] == c[(k, i, j)] for (k, j, i) in taps)
+    return {(1, False): 18.25, (1, True): 16.5, (2, False): 69.0, (2, True): 58.5}[(r, ij)]
 
 
 def cpu_baseline_on_device_data(B, s_in, s_out, info, interior, sts, shapes, lay, nbricks, bsize, sp, run_one):

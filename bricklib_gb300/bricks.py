@@ -254,6 +254,16 @@ class BrickStorage:
         call("bk_memset", C.c_void_p(buf.ptr), 0, buf.nbytes, None)
         return BrickStorage(chunks, step, dt, device=buf)
 
+    @staticmethod
+    def allocate_pinned(chunks: int, step: int, dtype=BK_F64) -> "BrickStorage":
+        """Storage in page-locked host memory mapped into the device (bk_host_malloc): `host` is
+        its numpy view and kernels use it at the same address, e.g. as a sweep's output field,
+        whose results then arrive in host memory without a separate copy."""
+        dt = dtype_of(dtype)
+        buf = PinnedBuffer(int(chunks) * int(step) * ELEM_SIZE[dt])
+        st = BrickStorage(chunks, step, dt, host=buf.view(NP_DTYPE[dt]), device=buf)
+        return st
+
     @property
     def nbytes(self) -> int:
         return self.chunks * self.step * ELEM_SIZE[self.dtype]

@@ -108,7 +108,17 @@ int bk_host_malloc(void **hptr, size_t bytes) {
   if (!hptr) return fail(BK_ERR_ARG, "hptr is NULL");
   *hptr = nullptr;
   if (bytes == 0) return BK_OK;
-  BK_CUDA(cudaMallocHost(hptr, bytes));
+  // mapped: kernels of this library may read or write it at the same address (an output field
+  // in this memory receives a sweep's results straight over the CPU-GPU link)
+  BK_CUDA(cudaHostAlloc(hptr, bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+  void *dptr = nullptr;
+  cudaError_t e = cudaHostGetDevicePointer(&dptr, *hptr, 0);
+  if (e != cudaSuccess || dptr != *hptr) {
+    cudaFreeHost(*hptr);
+    *hptr = nullptr;
+    return e != cudaSuccess ? cuda_fail(e, "cudaHostGetDevicePointer")
+                            : fail(BK_ERR_UNSUPPORTED, "page-locked memory is not at the same device address");
+  }
   return BK_OK;
 }
 

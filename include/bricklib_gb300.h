@@ -106,7 +106,10 @@ int bk_stream_synchronize(void *stream);
  * gpuFree deleter of the device BrickStorage (brick-gpu.h:97-101). */
 int bk_device_malloc(void **dptr, size_t bytes);
 int bk_device_free(void *dptr);
-/* Page-locked host memory for copies that overlap with kernels. */
+/* Page-locked host memory for copies that overlap with kernels.  It is mapped into the
+ * device's address space at the same address, so it can also hold a field that kernels
+ * of this library read or write directly: an output field in it receives a sweep's results
+ * straight over the CPU-GPU link (NVLink-C2C on GB300), with no separate device-to-host copy. */
 int bk_host_malloc(void **hptr, size_t bytes);
 int bk_host_free(void *hptr);
 /* Stream-ordered copy; kind: 0 host->device, 1 device->host, 2 device->device. */

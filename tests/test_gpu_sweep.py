@@ -297,6 +297,23 @@ def test_tma_star_kernel_equals_pipelined(dtype, acc, name, monkeypatch):
         assert int(np.count_nonzero((written != 0xFF).any(axis=1))) == nout
 
 
+@pytest.mark.parametrize("name,acc", [("star7", BK_ACC_NATIVE), ("cube27", BK_ACC_NATIVE),
+                                      ("cube125", _abi.BK_ACC_FLOATFLOAT)])
+def test_output_field_in_mapped_host_memory(name, acc, kernel):
+    """An output field in page-locked host memory (bk_host_malloc) receives exactly the
+    device sweep's results, written by the kernel over the CPU-GPU link."""
+    st = stencils.make(name, 5)
+    dom, arr, _ = device_sweep(32, st, acc=acc, seed=4)
+    hst = B.BrickStorage.allocate_pinned(dom.nbricks, dom.step)
+    hst.host[:] = 0
+    B.brickSweep(dom.brick(0), B.Brick(dom.dev_info, hst, dom.bsize), dom.dev_interior, st, acc)
+    B.synchronize()
+    assert B.error_flags() == 0
+    want = dom.storage.host.reshape(dom.nbricks, dom.step)[:, dom.bsize:][dom.interior]
+    got = hst.host.reshape(dom.nbricks, dom.step)[:, dom.bsize:][dom.interior]
+    np.testing.assert_array_equal(got, want)
+
+
 def test_empty_brick_list_is_a_no_op():
     dom = GridDomain(16)
     B.brickSweep(dom.brick(0), dom.brick(1), B.BrickList(np.zeros(0, np.uint32)), stencils.make("star7", 1))
