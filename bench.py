@@ -63,6 +63,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest value of x over the ranks of the job (the slowest replica's time); x itself
+    when the job has one rank.  Works on NCCL (device tensor) and gloo (host tensor) groups."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     try:
         with open(PEAKS_PATH) as f:
@@ -202,11 +214,7 @@ def run_ours(args):
         torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    total_ms = t0.elapsed_time(t1)
-    if ws > 1:
-        tt = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(t0.elapsed_time(t1))
     per_shape_ms = {name: sum(a.elapsed_time(b) for a, b in ev[name]) / K for name in shapes}
     ms_per_step = total_ms / K
     value = ws * len(shapes) * points / (ms_per_step * 1e-3) / 1e9
@@ -316,7 +324,7 @@ def run_ours(args):
             consumed[cur].record(stream)
         e1.record(stream)
         torch.cuda.synchronize()
-        e_ms = e0.elapsed_time(e1) / Ke
+        e_ms = max_over_ranks(e0.elapsed_time(e1) / Ke)
         # the host copy of the last result equals the device sweep's
         sweep(shapes[-1])
         dev_out = np.empty(nbricks * bsize, dtype=B.NP_DTYPE[dtype])
