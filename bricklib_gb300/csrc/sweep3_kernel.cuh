@@ -338,6 +338,32 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
         for (int kk = 0; kk < BK; ++kk) w[R + kk] = to_acc(f[eC + (kk * BJ + j) * BI + i]);
 #pragma unroll
         for (int kk = 0; kk < R; ++kk) w[R + BK + kk] = to_acc(f[eKH + (kk * BJ + j) * BI + i]);
+        if constexpr (ACC == ACCM_NATIVE && sizeof(AT) == 4) {
+          // two k planes per packed FP32 multiply-add (FFMA2): per point the same operations in
+          // the same order as the scalar path below, so the results are identical
+          static_assert(BK % 2 == 0, "k planes in pairs");
+          auto cc = [&](int t) {
+            const float c = coef<float>(tp, t);
+            return make_float2(c, c);
+          };
+#pragma unroll
+          for (int k = 0; k < BK; k += 2) {
+            auto ld2 = [&](int o, int st) { return make_float2(to_acc(f[o + k * st]), to_acc(f[o + (k + 1) * st])); };
+            float2 v = __fmul2_rn(cc(0), make_float2(w[k + R], w[k + R + 1]));
+#pragma unroll
+            for (int d = 1; d <= R; ++d) {
+              const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+              v = __ffma2_rn(cc(t + 0), ld2(oi[q], si[q]), v);
+              v = __ffma2_rn(cc(t + 1), ld2(oi[q + 1], si[q + 1]), v);
+              v = __ffma2_rn(cc(t + 2), ld2(oj[q], sj[q]), v);
+              v = __ffma2_rn(cc(t + 3), ld2(oj[q + 1], sj[q + 1]), v);
+              v = __ffma2_rn(cc(t + 4), make_float2(w[k + R + d], w[k + R + 1 + d]), v);
+              v = __ffma2_rn(cc(t + 5), make_float2(w[k + R - d], w[k + R + 1 - d]), v);
+            }
+            store_stream(ob + k * PK, v.x);
+            store_stream(ob + (k + 1) * PK, v.y);
+          }
+        } else
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
           AT v;
