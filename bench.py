@@ -280,35 +280,41 @@ def run_ours(args):
         tot = sum(v["ms"] for v in alt["per_stencil"].values())
         alt["value"] = round(len(shapes) * points / (tot * 1e-3) / 1e9, 3)
 
-    # end to end through the public API: pinned host input -> device (copy), sweeps whose output
-    # field is page-locked host memory (bk_host_malloc, mapped): each result is stored into host
-    # memory by the sweep itself, over NVLink-C2C, with no separate device-to-host copy.  Two
-    # device input buffers: the input of step t+1 is copied on a second stream while step t
-    # sweeps (the link carries the copy and the results in opposite directions).
+    # end to end through the public API, every result in host memory.  Per step: the input is
+    # copied from page-locked memory (on a copy stream, into one of two device buffers, while the
+    # previous step sweeps); each sweep but the last writes a device buffer (two, ping-pong) whose
+    # device-to-host copy runs on a second copy stream under the next sweep; the last sweep
+    # stores its result straight into mapped page-locked host memory (bk_host_malloc) over
+    # NVLink-C2C.  The link carries the input and the results in opposite directions.
     e2e = None
     if not args.no_e2e:
         nbytes = nbricks * bsize * esize
         h_in = B.PinnedBuffer(nbytes)
         s_in2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
         ins = [B.Brick(dinfo, s_in, 0, lay), B.Brick(dinfo, s_in2, 0, lay)]
-        s_hout = B.BrickStorage.allocate_pinned(nbricks, bsize, dtype)
-        s_hout.host[:] = 0
-        b_hout = B.Brick(dinfo, s_hout, 0, lay)
+        s_out2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
+        outs = [B.Brick(dinfo, s_out, 0, lay), B.Brick(dinfo, s_out2, 0, lay)]
+        h_outs = {}
+        for name in shapes:
+            h_outs[name] = B.BrickStorage.allocate_pinned(nbricks, bsize, dtype)
+            h_outs[name].host[:] = 0
         B.memcpy(h_in.ptr, s_in.ptr, nbytes, 1, sp)
         torch.cuda.synchronize()
-        cstream = torch.cuda.Stream()
+        cin, cout = torch.cuda.Stream(), torch.cuda.Stream()
         arrived = [torch.cuda.Event(), torch.cuda.Event()]
         consumed = [torch.cuda.Event(), torch.cuda.Event()]
+        swept = [torch.cuda.Event(), torch.cuda.Event()]
+        copied = [torch.cuda.Event(), torch.cuda.Event()]
         Ke = max(1, min(K, 5))
 
         def h2d(buf):
-            with torch.cuda.stream(cstream):
-                cstream.wait_event(consumed[buf])
-                B.memcpy(ins[buf].bStorage.ptr, h_in.ptr, nbytes, 0, cstream.cuda_stream)
-                arrived[buf].record(cstream)
+            cin.wait_event(consumed[buf])
+            B.memcpy(ins[buf].bStorage.ptr, h_in.ptr, nbytes, 0, cin.cuda_stream)
+            arrived[buf].record(cin)
 
         for q in range(2):
             consumed[q].record(stream)
+            copied[q].record(stream)
         h2d(0)
         for it in range(Ke + 1):
             cur = it % 2
@@ -319,24 +325,37 @@ def run_ours(args):
             if it < Ke:
                 h2d(1 - cur)  # the next step's input, while this step sweeps
             stream.wait_event(arrived[cur])
-            for name in shapes:
-                B.brickSweep(ins[cur], b_hout, blist, csts[name], acc, stream=sp)
+            for q, name in enumerate(shapes):
+                if q == len(shapes) - 1:
+                    B.brickSweep(ins[cur], B.Brick(dinfo, h_outs[name], 0, lay), blist, csts[name], acc, stream=sp)
+                    continue
+                ob = q % 2
+                stream.wait_event(copied[ob])  # its previous result has left the buffer
+                B.brickSweep(ins[cur], outs[ob], blist, csts[name], acc, stream=sp)
+                swept[ob].record(stream)
+                cout.wait_event(swept[ob])
+                B.memcpy(h_outs[name].ptr, outs[ob].bStorage.ptr, nbytes, 1, cout.cuda_stream)
+                copied[ob].record(cout)
             consumed[cur].record(stream)
+        for q in range(2):
+            stream.wait_event(copied[q])
         e1.record(stream)
         torch.cuda.synchronize()
         e_ms = max_over_ranks(e0.elapsed_time(e1) / Ke)
-        # the host copy of the last result equals the device sweep's
-        sweep(shapes[-1])
+        # every host result equals the device sweep's
         dev_out = np.empty(nbricks * bsize, dtype=B.NP_DTYPE[dtype])
-        B.memcpy(dev_out.ctypes.data, s_out.ptr, nbytes, 1, sp)
-        B.synchronize(sp)
-        if not np.array_equal(dev_out.view(np.uint8), s_hout.host.view(np.uint8)):
-            raise RuntimeError("sweep into host memory differs from the device sweep")
+        for name in shapes:
+            sweep(name)
+            B.memcpy(dev_out.ctypes.data, s_out.ptr, nbytes, 1, sp)
+            B.synchronize(sp)
+            if not np.array_equal(dev_out.view(np.uint8), h_outs[name].host.view(np.uint8)):
+                raise RuntimeError(f"{name}: the result in host memory differs from the device sweep")
         e2e = {"value": round(ws * len(shapes) * points / (e_ms * 1e-3) / 1e9, 3), "unit": "GStencil/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3),
-               "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a "
-                       "copy stream, overlapped with the previous step's sweeps; results: stored by each sweep "
-                       "into mapped page-locked host memory over NVLink-C2C"}
+               "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a copy "
+                       "stream under the previous step's sweeps; results: device-to-host copies on a second "
+                       "stream under the next sweep, the last sweep storing straight into mapped page-locked "
+                       "host memory over NVLink-C2C; one host buffer per stencil"}
 
     # CPU baseline: the oracle's OpenMP brick sweep on a sample of the same bricks,
     # also used as a spot check of the GPU output on those bricks
