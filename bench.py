@@ -448,10 +448,11 @@ def run_reference(args):
     from oracle import oracle
     oracle.build()
     shapes = args.shapes.split(",")
-    # the reference's CPU brick path, timed on a 64^3-interior sample of the workload per
-    # shape per step (same bricks, fold and taps; the reference-compiled build does not
-    # travel to an aarch64 host, so the OpenMP restatement of it runs here)
-    m = 64
+    # the reference's CPU brick path, timed on a 256^3-interior sample of the workload per
+    # shape per step (same bricks, fold and taps; large enough that the OpenMP brick loop, not
+    # the per-call overhead, sets the rate; the reference-compiled build does not travel to an
+    # aarch64 host, so the OpenMP restatement of it runs here)
+    m = 256
     dom = oracle.Domain(m)
     arr = stencils.uniform(SEED_IN, int(np.prod(dom.adims))).reshape(dom.adims)
     dat = dom.alloc()
