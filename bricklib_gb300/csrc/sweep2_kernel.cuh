@@ -179,13 +179,226 @@ __device__ __forceinline__ unsigned plan_entry(int g) {
   return slot | (src << 5) | (dst << 18);
 }
 
+// One brick's outputs from its staged tile (the compute of sweep2_kernel, shared with the
+// warp-specialised kernel): each of the BJ*BI threads (lt) owns one (j, i) column.
+// out_brick: the output field's brick (field base + centre brick x step).
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
+__device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, const Taps &tp) {
+  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
+  typedef typename Elem<T>::acc AT;
+  constexpr int EJ = C::EJ, EI = C::EI, SK = EJ * EI, SJ = EI, RP = C::RP;
+  int j = lt / BI;
+  const int i = lt - j * BI;
+  if (C::PERM) j = (j & ~3) | ((j & 1) << 1) | ((j >> 1) & 1);  // rows 0,2,1,3 per warp
+  T *ob = out_brick + (size_t)(j * BI + i);
+  const int cofs = (j + R) * SJ + (i + RP);  // column (j, i) at kk = 0
+  if constexpr (ACC == ACCM_FF) {
+    const float2 *ft = reinterpret_cast<const float2 *>(rt);
+    if constexpr (FAM == FAM_STAR) {
+      float2 w[BK + 2 * R];
+#pragma unroll
+      for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = ft[kk * SK + cofs];
+#pragma unroll
+      for (int k = 0; k < BK; ++k) {
+        const float2 *c = ft + (k + R) * SK + cofs;
+        FFAcc acc;
+        acc.first(tp.cf[0], tp.cl[0], w[k + R]);
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          const int t = 1 + 6 * (d - 1);
+          acc.add(tp.cf[t + 0], tp.cl[t + 0], c[d]);
+          acc.add(tp.cf[t + 1], tp.cl[t + 1], c[-d]);
+          acc.add(tp.cf[t + 2], tp.cl[t + 2], c[d * SJ]);
+          acc.add(tp.cf[t + 3], tp.cl[t + 3], c[-d * SJ]);
+          acc.add(tp.cf[t + 4], tp.cl[t + 4], w[k + R + d]);
+          acc.add(tp.cf[t + 5], tp.cl[t + 5], w[k + R - d]);
+          acc.renorm();
+        }
+        store_stream(ob + k * BJ * BI, acc.result());
+      }
+    } else if constexpr (FAM == FAM_CUBE) {
+      FFAcc acc[BK];
+#pragma unroll
+      for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+        for (int di = -R; di <= R; ++di) {
+          float2 w[BK + 2 * R];
+#pragma unroll
+          for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = ft[kk * SK + cofs + dj * SJ + di];
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+#pragma unroll
+            for (int dk = -R; dk <= R; ++dk) {
+              const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+              if (dj == -R && di == -R && dk == -R) acc[k].first(tp.cf[t], tp.cl[t], w[k + R + dk]);
+              else acc[k].add(tp.cf[t], tp.cl[t], w[k + R + dk]);
+            }
+            acc[k].renorm();
+          }
+        }
+#pragma unroll
+      for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k].result());
+    } else {
+#pragma unroll 1
+      for (int k = 0; k < BK; ++k) {
+        const float2 *c = ft + (k + R) * SK + cofs;
+        FFAcc acc;
+        acc.first(tp.cf[0], tp.cl[0], c[tp.toff[0]]);
+        for (int t = 1; t < tp.n; ++t) {
+          acc.add(tp.cf[t], tp.cl[t], c[tp.toff[t]]);
+          if ((t & 7) == 7) acc.renorm();
+        }
+        store_stream(ob + k * BJ * BI, acc.result());
+      }
+    }
+  } else {
+    if constexpr (FAM == FAM_STAR) {
+      AT w[BK + 2 * R];
+#pragma unroll
+      for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = to_acc(rt[kk * SK + cofs]);
+#pragma unroll
+      for (int k = 0; k < BK; ++k) {
+        const T *c = rt + (k + R) * SK + cofs;
+        AT v;
+        if constexpr (ACC == ACCM_NATIVE) {
+          v = coef<AT>(tp, 0) * w[k + R];
+#pragma unroll
+          for (int d = 1; d <= R; ++d) {
+            const int t = 1 + 6 * (d - 1);
+            v = fma(coef<AT>(tp, t + 0), to_acc(c[d]), v);
+            v = fma(coef<AT>(tp, t + 1), to_acc(c[-d]), v);
+            v = fma(coef<AT>(tp, t + 2), to_acc(c[d * SJ]), v);
+            v = fma(coef<AT>(tp, t + 3), to_acc(c[-d * SJ]), v);
+            v = fma(coef<AT>(tp, t + 4), w[k + R + d], v);
+            v = fma(coef<AT>(tp, t + 5), w[k + R - d], v);
+          }
+        } else {
+          AT row = coef<AT>(tp, 0) * w[k + R];
+#pragma unroll
+          for (int d = 1; d <= R; ++d) {
+            const int t = 1 + 6 * (d - 1);
+            row = fma(coef<AT>(tp, t + 0), to_acc(c[d]), row);
+            row = fma(coef<AT>(tp, t + 1), to_acc(c[-d]), row);
+          }
+          AT s = row, comp = AT(0);
+#pragma unroll
+          for (int d = 1; d <= R; ++d) {
+            const int t = 1 + 6 * (d - 1);
+            neumaier(s, comp, coef<AT>(tp, t + 2) * to_acc(c[d * SJ]));
+            neumaier(s, comp, coef<AT>(tp, t + 3) * to_acc(c[-d * SJ]));
+            neumaier(s, comp, coef<AT>(tp, t + 4) * w[k + R + d]);
+            neumaier(s, comp, coef<AT>(tp, t + 5) * w[k + R - d]);
+          }
+          v = s + comp;
+        }
+        store_stream(ob + k * BJ * BI, v);
+      }
+    } else if constexpr (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ) {
+      // Mirror-symmetric cube: for every (b, a) = (|dj|, |di|) the column
+      //   q[kk] = sum of x(kk, j +- b, i +- a) over the distinct sign choices
+      // is formed with additions, then
+      //   out(k) += c(0,b,a) q[k] + sum_{c>=1} c(c,b,a) (q[k-c] + q[k+c]).
+      // Per point: 69 instead of 125 floating-point operations for R = 2 (27 multiply-adds,
+      // 42 additions), 18 instead of 27 for R = 1.  With the i <-> j swap symmetry the
+      // columns of (b, a) and (a, b) share their coefficients and are added first: 58.5
+      // operations for R = 2.
+      static_assert(ACC == ACCM_NATIVE, "symmetric cubes: native arithmetic");
+      constexpr bool IJ = FAM == FAM_CUBESYM_IJ;
+      AT acc[BK];
+      // sum of x(kk, j +- b, i +- a) over the distinct sign choices
+      auto ring = [&](const T *c, int b, int a) -> AT {
+        if (a == 0 && b == 0) return to_acc(c[0]);
+        if (b == 0) return to_acc(c[-a]) + to_acc(c[a]);
+        if (a == 0) return to_acc(c[-b * SJ]) + to_acc(c[b * SJ]);
+        return (to_acc(c[-b * SJ - a]) + to_acc(c[-b * SJ + a])) + (to_acc(c[b * SJ - a]) + to_acc(c[b * SJ + a]));
+      };
+#pragma unroll
+      for (int b = 0; b <= R; ++b)
+#pragma unroll
+        for (int a = 0; a <= (IJ ? b : R); ++a) {
+          AT q[BK + 2 * R];
+#pragma unroll
+          for (int kk = 0; kk < BK + 2 * R; ++kk) {
+            const T *c = rt + kk * SK + cofs;
+            q[kk] = (IJ && a != b) ? ring(c, b, a) + ring(c, a, b) : ring(c, b, a);
+          }
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            const AT c0 = coef<AT>(tp, sym_index(0, b, a, R));
+            if (a == 0 && b == 0) acc[k] = c0 * q[k + R];
+            else acc[k] = fma(c0, q[k + R], acc[k]);
+#pragma unroll
+            for (int d = 1; d <= R; ++d)
+              acc[k] = fma(coef<AT>(tp, sym_index(d, b, a, R)), q[k + R - d] + q[k + R + d], acc[k]);
+          }
+        }
+#pragma unroll
+      for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k]);
+    } else if constexpr (FAM == FAM_CUBE) {
+      AT acc[BK], comp[BK];
+#pragma unroll
+      for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+        for (int di = -R; di <= R; ++di) {
+          AT w[BK + 2 * R];
+#pragma unroll
+          for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = to_acc(rt[kk * SK + cofs + dj * SJ + di]);
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            if constexpr (ACC == ACCM_NATIVE) {
+#pragma unroll
+              for (int dk = -R; dk <= R; ++dk) {
+                const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+                if (dj == -R && di == -R && dk == -R) acc[k] = coef<AT>(tp, t) * w[k + R + dk];
+                else acc[k] = fma(coef<AT>(tp, t), w[k + R + dk], acc[k]);
+              }
+            } else {
+              // the 2R+1 k taps of this column as one FMA chain, columns Neumaier-summed
+              const int t0 = ((0) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+              AT col = coef<AT>(tp, t0) * w[k];
+#pragma unroll
+              for (int dk = -R + 1; dk <= R; ++dk) {
+                const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+                col = fma(coef<AT>(tp, t), w[k + R + dk], col);
+              }
+              if (dj == -R && di == -R) {
+                acc[k] = col;
+                comp[k] = AT(0);
+              } else {
+                neumaier(acc[k], comp[k], col);
+              }
+            }
+          }
+        }
+#pragma unroll
+      for (int k = 0; k < BK; ++k) {
+        if constexpr (ACC == ACCM_NATIVE) store_stream(ob + k * BJ * BI, acc[k]);
+        else store_stream(ob + k * BJ * BI, acc[k] + comp[k]);
+      }
+    } else {
+#pragma unroll 1
+      for (int k = 0; k < BK; ++k) {
+        const T *c = rt + (k + R) * SK + cofs;
+        AT v;
+        if constexpr (ACC == ACCM_NATIVE) {
+          v = coef<AT>(tp, 0) * to_acc(c[tp.toff[0]]);
+          for (int t = 1; t < tp.n; ++t) v = fma(coef<AT>(tp, t), to_acc(c[tp.toff[t]]), v);
+        } else {
+          AT s = coef<AT>(tp, 0) * to_acc(c[tp.toff[0]]), comp = AT(0);
+          for (int t = 1; t < tp.n; ++t) neumaier(s, comp, coef<AT>(tp, t) * to_acc(c[tp.toff[t]]));
+          v = s + comp;
+        }
+        store_stream(ob + k * BJ * BI, v);
+      }
+    }
+  }
+}
+
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH>
 __global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC>::NT)
 sweep2_kernel(const SweepArgs a, const Taps tp) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
-  typedef typename Elem<T>::acc AT;
   constexpr int TPB = C::TPB, NB = C::NB, EPT = C::EPT;
-  constexpr int EJ = C::EJ, EI = C::EI, SK = EJ * EI, SJ = EI, RP = C::RP;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
@@ -330,213 +543,9 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
       __syncthreads();
     }
     if (active) {
-      int j = lt / BI;
-      const int i = lt - j * BI;
-      if (C::PERM) j = (j & ~3) | ((j & 1) << 1) | ((j >> 1) & 1);  // rows 0,2,1,3 per warp
       T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
       const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
-      T *ob = out + (size_t)nbr[13] * ostep + (size_t)(j * BI + i);
-      const int cofs = (j + R) * SJ + (i + RP);  // column (j, i) at kk = 0
-      if constexpr (ACC == ACCM_FF) {
-        const float2 *ft = reinterpret_cast<const float2 *>(rt);
-        if constexpr (FAM == FAM_STAR) {
-          float2 w[BK + 2 * R];
-#pragma unroll
-          for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = ft[kk * SK + cofs];
-#pragma unroll
-          for (int k = 0; k < BK; ++k) {
-            const float2 *c = ft + (k + R) * SK + cofs;
-            FFAcc acc;
-            acc.first(tp.cf[0], tp.cl[0], w[k + R]);
-#pragma unroll
-            for (int d = 1; d <= R; ++d) {
-              const int t = 1 + 6 * (d - 1);
-              acc.add(tp.cf[t + 0], tp.cl[t + 0], c[d]);
-              acc.add(tp.cf[t + 1], tp.cl[t + 1], c[-d]);
-              acc.add(tp.cf[t + 2], tp.cl[t + 2], c[d * SJ]);
-              acc.add(tp.cf[t + 3], tp.cl[t + 3], c[-d * SJ]);
-              acc.add(tp.cf[t + 4], tp.cl[t + 4], w[k + R + d]);
-              acc.add(tp.cf[t + 5], tp.cl[t + 5], w[k + R - d]);
-              acc.renorm();
-            }
-            store_stream(ob + k * BJ * BI, acc.result());
-          }
-        } else if constexpr (FAM == FAM_CUBE) {
-          FFAcc acc[BK];
-#pragma unroll
-          for (int dj = -R; dj <= R; ++dj)
-#pragma unroll
-            for (int di = -R; di <= R; ++di) {
-              float2 w[BK + 2 * R];
-#pragma unroll
-              for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = ft[kk * SK + cofs + dj * SJ + di];
-#pragma unroll
-              for (int k = 0; k < BK; ++k) {
-#pragma unroll
-                for (int dk = -R; dk <= R; ++dk) {
-                  const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
-                  if (dj == -R && di == -R && dk == -R) acc[k].first(tp.cf[t], tp.cl[t], w[k + R + dk]);
-                  else acc[k].add(tp.cf[t], tp.cl[t], w[k + R + dk]);
-                }
-                acc[k].renorm();
-              }
-            }
-#pragma unroll
-          for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k].result());
-        } else {
-#pragma unroll 1
-          for (int k = 0; k < BK; ++k) {
-            const float2 *c = ft + (k + R) * SK + cofs;
-            FFAcc acc;
-            acc.first(tp.cf[0], tp.cl[0], c[tp.toff[0]]);
-            for (int t = 1; t < tp.n; ++t) {
-              acc.add(tp.cf[t], tp.cl[t], c[tp.toff[t]]);
-              if ((t & 7) == 7) acc.renorm();
-            }
-            store_stream(ob + k * BJ * BI, acc.result());
-          }
-        }
-      } else {
-        if constexpr (FAM == FAM_STAR) {
-          AT w[BK + 2 * R];
-#pragma unroll
-          for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = to_acc(rt[kk * SK + cofs]);
-#pragma unroll
-          for (int k = 0; k < BK; ++k) {
-            const T *c = rt + (k + R) * SK + cofs;
-            AT v;
-            if constexpr (ACC == ACCM_NATIVE) {
-              v = coef<AT>(tp, 0) * w[k + R];
-#pragma unroll
-              for (int d = 1; d <= R; ++d) {
-                const int t = 1 + 6 * (d - 1);
-                v = fma(coef<AT>(tp, t + 0), to_acc(c[d]), v);
-                v = fma(coef<AT>(tp, t + 1), to_acc(c[-d]), v);
-                v = fma(coef<AT>(tp, t + 2), to_acc(c[d * SJ]), v);
-                v = fma(coef<AT>(tp, t + 3), to_acc(c[-d * SJ]), v);
-                v = fma(coef<AT>(tp, t + 4), w[k + R + d], v);
-                v = fma(coef<AT>(tp, t + 5), w[k + R - d], v);
-              }
-            } else {
-              AT row = coef<AT>(tp, 0) * w[k + R];
-#pragma unroll
-              for (int d = 1; d <= R; ++d) {
-                const int t = 1 + 6 * (d - 1);
-                row = fma(coef<AT>(tp, t + 0), to_acc(c[d]), row);
-                row = fma(coef<AT>(tp, t + 1), to_acc(c[-d]), row);
-              }
-              AT s = row, comp = AT(0);
-#pragma unroll
-              for (int d = 1; d <= R; ++d) {
-                const int t = 1 + 6 * (d - 1);
-                neumaier(s, comp, coef<AT>(tp, t + 2) * to_acc(c[d * SJ]));
-                neumaier(s, comp, coef<AT>(tp, t + 3) * to_acc(c[-d * SJ]));
-                neumaier(s, comp, coef<AT>(tp, t + 4) * w[k + R + d]);
-                neumaier(s, comp, coef<AT>(tp, t + 5) * w[k + R - d]);
-              }
-              v = s + comp;
-            }
-            store_stream(ob + k * BJ * BI, v);
-          }
-        } else if constexpr (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ) {
-          // Mirror-symmetric cube: for every (b, a) = (|dj|, |di|) the column
-          //   q[kk] = sum of x(kk, j +- b, i +- a) over the distinct sign choices
-          // is formed with additions, then
-          //   out(k) += c(0,b,a) q[k] + sum_{c>=1} c(c,b,a) (q[k-c] + q[k+c]).
-          // Per point: 69 instead of 125 floating-point operations for R = 2 (27 multiply-adds,
-          // 42 additions), 18 instead of 27 for R = 1.  With the i <-> j swap symmetry the
-          // columns of (b, a) and (a, b) share their coefficients and are added first: 58.5
-          // operations for R = 2.
-          static_assert(ACC == ACCM_NATIVE, "symmetric cubes: native arithmetic");
-          constexpr bool IJ = FAM == FAM_CUBESYM_IJ;
-          AT acc[BK];
-          // sum of x(kk, j +- b, i +- a) over the distinct sign choices
-          auto ring = [&](const T *c, int b, int a) -> AT {
-            if (a == 0 && b == 0) return to_acc(c[0]);
-            if (b == 0) return to_acc(c[-a]) + to_acc(c[a]);
-            if (a == 0) return to_acc(c[-b * SJ]) + to_acc(c[b * SJ]);
-            return (to_acc(c[-b * SJ - a]) + to_acc(c[-b * SJ + a])) + (to_acc(c[b * SJ - a]) + to_acc(c[b * SJ + a]));
-          };
-#pragma unroll
-          for (int b = 0; b <= R; ++b)
-#pragma unroll
-            for (int a = 0; a <= (IJ ? b : R); ++a) {
-              AT q[BK + 2 * R];
-#pragma unroll
-              for (int kk = 0; kk < BK + 2 * R; ++kk) {
-                const T *c = rt + kk * SK + cofs;
-                q[kk] = (IJ && a != b) ? ring(c, b, a) + ring(c, a, b) : ring(c, b, a);
-              }
-#pragma unroll
-              for (int k = 0; k < BK; ++k) {
-                const AT c0 = coef<AT>(tp, sym_index(0, b, a, R));
-                if (a == 0 && b == 0) acc[k] = c0 * q[k + R];
-                else acc[k] = fma(c0, q[k + R], acc[k]);
-#pragma unroll
-                for (int d = 1; d <= R; ++d)
-                  acc[k] = fma(coef<AT>(tp, sym_index(d, b, a, R)), q[k + R - d] + q[k + R + d], acc[k]);
-              }
-            }
-#pragma unroll
-          for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k]);
-        } else if constexpr (FAM == FAM_CUBE) {
-          AT acc[BK], comp[BK];
-#pragma unroll
-          for (int dj = -R; dj <= R; ++dj)
-#pragma unroll
-            for (int di = -R; di <= R; ++di) {
-              AT w[BK + 2 * R];
-#pragma unroll
-              for (int kk = 0; kk < BK + 2 * R; ++kk) w[kk] = to_acc(rt[kk * SK + cofs + dj * SJ + di]);
-#pragma unroll
-              for (int k = 0; k < BK; ++k) {
-                if constexpr (ACC == ACCM_NATIVE) {
-#pragma unroll
-                  for (int dk = -R; dk <= R; ++dk) {
-                    const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
-                    if (dj == -R && di == -R && dk == -R) acc[k] = coef<AT>(tp, t) * w[k + R + dk];
-                    else acc[k] = fma(coef<AT>(tp, t), w[k + R + dk], acc[k]);
-                  }
-                } else {
-                  // the 2R+1 k taps of this column as one FMA chain, columns Neumaier-summed
-                  const int t0 = ((0) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
-                  AT col = coef<AT>(tp, t0) * w[k];
-#pragma unroll
-                  for (int dk = -R + 1; dk <= R; ++dk) {
-                    const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
-                    col = fma(coef<AT>(tp, t), w[k + R + dk], col);
-                  }
-                  if (dj == -R && di == -R) {
-                    acc[k] = col;
-                    comp[k] = AT(0);
-                  } else {
-                    neumaier(acc[k], comp[k], col);
-                  }
-                }
-              }
-            }
-#pragma unroll
-          for (int k = 0; k < BK; ++k) {
-            if constexpr (ACC == ACCM_NATIVE) store_stream(ob + k * BJ * BI, acc[k]);
-            else store_stream(ob + k * BJ * BI, acc[k] + comp[k]);
-          }
-        } else {
-#pragma unroll 1
-          for (int k = 0; k < BK; ++k) {
-            const T *c = rt + (k + R) * SK + cofs;
-            AT v;
-            if constexpr (ACC == ACCM_NATIVE) {
-              v = coef<AT>(tp, 0) * to_acc(c[tp.toff[0]]);
-              for (int t = 1; t < tp.n; ++t) v = fma(coef<AT>(tp, t), to_acc(c[tp.toff[t]]), v);
-            } else {
-              AT s = coef<AT>(tp, 0) * to_acc(c[tp.toff[0]]), comp = AT(0);
-              for (int t = 1; t < tp.n; ++t) neumaier(s, comp, coef<AT>(tp, t) * to_acc(c[tp.toff[t]]));
-              v = s + comp;
-            }
-            store_stream(ob + k * BJ * BI, v);
-          }
-        }
-      }
+      sweep2_brick<T, BK, BJ, BI, R, FAM, ACC>(rt, out + (size_t)nbr[13] * ostep, lt, tp);
     }
     store_adj(nfar);  // group it + 2; read after the next iteration's first barrier
   }

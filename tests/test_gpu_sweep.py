@@ -88,6 +88,16 @@ def test_fp64_matches_oracle_64(name, kernel):
     assert ok, f"{name}: max |diff| {md}"
 
 
+def test_c1_laplacian_128():
+    """The reference's CPU-runnable case: 7-point Laplacian (centre -6/h^2, axes 1/h^2, h = 1/128),
+    FP64, 128^3 interior + 8-cell ghost, uniform[-1,1) input, one sweep, checked against the array
+    kernel with compareBrick's mixed test."""
+    st = stencils.make("lap7")
+    dom, arr, got = device_sweep(128, st, seed=20261204)
+    ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+    assert ok, f"max |diff| {md}"
+
+
 LAYOUTS = [((8, 8, 8), (1, 1, 8)), ((8, 8, 8), (1, 2, 2)), ((8, 8, 8), (2, 4, 4)), ((4, 4, 4), (1, 4, 4)),
            ((16, 8, 8), (1, 4, 8)), ((8, 8, 32), (1, 1, 32)), ((8, 8, 32), (1, 4, 8))]
 
