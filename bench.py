@@ -248,6 +248,9 @@ def run_ours(args):
                             "note": "achieved counts 2 x taps flop per point; pipe_frac counts the floating-point "
                                     "instructions the kernel executes per point (mirror-symmetric cubes run on "
                                     "pair sums) against the measured FMA instruction rate"}}
+    pipe_frac = roofline["compute"]["pipe_frac"]
+    roofline["binding"] = (("fp64 pipe" if dtype == _abi.BK_F64 and acc != _abi.BK_ACC_FLOATFLOAT else "fp32 pipe")
+                           if pipe_frac > roofline["frac"] else "hbm")
 
     # the other FP64 arithmetic mode on the same data: per-stencil rate and its normwise
     # error against the first mode's output
