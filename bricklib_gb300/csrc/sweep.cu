@@ -163,7 +163,9 @@ static int plan_sweep(const bk_field *in, const bk_field *out, const bk_stencil 
     // float-float cubes and the radius-4 star are bound by the FP32 pipes; the one-shot
     // kernel's single tile buffer keeps twice as many CTAs resident and wins there
     // (measured on GB300: cube125 18.6 vs 12.8, cube27 61 vs 46, star25 17 vs 15 GStencil/s)
-    if (plan->acc == ACCM_FF && (plan->fam == FAM_CUBE || plan->r >= 4) && !getenv("BK_SWEEP_PIPELINED"))
+    // (mirror-symmetric float-float cubes, on pair sums, stay on the pipelined kernel)
+    if (plan->acc == ACCM_FF && ((plan->fam == FAM_CUBE && !(plan->sym && plan->shape == 0)) || plan->r >= 4) &&
+        !getenv("BK_SWEEP_PIPELINED"))
       plan->v2 = false;
     // star stencils on 8x8x8 row-major bricks: the TMA-fed kernel, unless a kernel is forced
     plan->tma = tma_eligible(*plan, in) && !getenv("BK_SWEEP_ONESHOT") && !getenv("BK_SWEEP_PIPELINED");
@@ -242,7 +244,8 @@ int bk_sweep_kernel(const bk_field *in, const bk_field *out, const bk_stencil *s
   if (!name) return fail(BK_ERR_ARG, "name is NULL");
   SweepPlan plan{};
   Layout L;
-  int s = plan_sweep(in, out, st, lay, acc, &plan, nullptr, &L);
+  static thread_local Taps tp;  // the coefficient analysis decides the symmetric-cube routes
+  int s = plan_sweep(in, out, st, lay, acc, &plan, &tp, &L);
   if (s) return s;
   *name = plan.tma ? "sweep_star_tma_kernel" : plan.v2 ? "sweep2_kernel" : "sweep_kernel";
   return BK_OK;

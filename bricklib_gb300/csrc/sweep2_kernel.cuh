@@ -238,6 +238,42 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
         }
 #pragma unroll
       for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k].result());
+    } else if constexpr (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ) {
+      // mirror-symmetric cube in float-float: the pair-sum evaluation of the native path below
+      // with float-float additions and Dot2 products
+      constexpr bool IJ = FAM == FAM_CUBESYM_IJ;
+      FFAcc acc[BK];
+      auto ring = [&](const float2 *c, int b, int a) -> float2 {
+        if (a == 0 && b == 0) return c[0];
+        if (b == 0) return ff_add(c[-a], c[a]);
+        if (a == 0) return ff_add(c[-b * SJ], c[b * SJ]);
+        return ff_add(ff_add(c[-b * SJ - a], c[-b * SJ + a]), ff_add(c[b * SJ - a], c[b * SJ + a]));
+      };
+#pragma unroll
+      for (int b = 0; b <= R; ++b)
+#pragma unroll
+        for (int a = 0; a <= (IJ ? b : R); ++a) {
+          float2 q[BK + 2 * R];
+#pragma unroll
+          for (int kk = 0; kk < BK + 2 * R; ++kk) {
+            const float2 *c = ft + kk * SK + cofs;
+            q[kk] = (IJ && a != b) ? ff_add(ring(c, b, a), ring(c, a, b)) : ring(c, b, a);
+          }
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            const int t0 = sym_index(0, b, a, R);
+            if (a == 0 && b == 0) acc[k].first(tp.cf[t0], tp.cl[t0], q[k + R]);
+            else acc[k].add(tp.cf[t0], tp.cl[t0], q[k + R]);
+#pragma unroll
+            for (int d = 1; d <= R; ++d) {
+              const int t = sym_index(d, b, a, R);
+              acc[k].add(tp.cf[t], tp.cl[t], ff_add(q[k + R - d], q[k + R + d]));
+            }
+            acc[k].renorm();
+          }
+        }
+#pragma unroll
+      for (int k = 0; k < BK; ++k) store_stream(ob + k * BJ * BI, acc[k].result());
     } else {
 #pragma unroll 1
       for (int k = 0; k < BK; ++k) {

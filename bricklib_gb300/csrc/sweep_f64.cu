@@ -46,6 +46,12 @@ int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStr
         if (p.r == 1) return launch_sweep2<double, 8, 8, 8, 1, FAM_CUBESYM, ACCM_NATIVE>(a, tp, s);
         if (p.r == 2) return launch_sweep2<double, 8, 8, 8, 2, FAM_CUBESYM, ACCM_NATIVE>(a, tp, s);
       }
+      if (p.sym && p.fam == FAM_CUBE && p.acc == ACCM_FF) {
+        if (p.symij && p.r == 1) return launch_sweep2<double, 8, 8, 8, 1, FAM_CUBESYM_IJ, ACCM_FF>(a, tp, s);
+        if (p.symij && p.r == 2) return launch_sweep2<double, 8, 8, 8, 2, FAM_CUBESYM_IJ, ACCM_FF>(a, tp, s);
+        if (p.r == 1) return launch_sweep2<double, 8, 8, 8, 1, FAM_CUBESYM, ACCM_FF>(a, tp, s);
+        if (p.r == 2) return launch_sweep2<double, 8, 8, 8, 2, FAM_CUBESYM, ACCM_FF>(a, tp, s);
+      }
       BK_SHAPE_SET2(8, 8, 8, ACCM_NATIVE)
       BK_SHAPE_SET2(8, 8, 8, ACCM_FF)
     } else if (p.shape == 1) {

@@ -169,6 +169,16 @@ __device__ __forceinline__ double ff_to_f64(float h, float l) {
   return __longlong_as_double((long long)bits);
 }
 
+// Float-float sum a + b (both hi + lo pairs): TwoSum of the high parts, the low parts and the
+// rounding error added, then renormalised with the fast two-sum.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  float s, e;
+  two_sum(a.x, b.x, s, e);
+  e += a.y + b.y;
+  const float h = s + e;
+  return make_float2(h, e - (h - s));
+}
+
 // Dot2-style accumulation of c * x: (s, corr) with s + corr ~ sum of products.
 struct FFAcc {
   float s, corr;

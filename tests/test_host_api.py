@@ -74,6 +74,8 @@ def test_kernel_choice(monkeypatch):
     assert _kernel_for("cube27") == "sweep2_kernel"
     assert _kernel_for("cube125", dtype=_abi.BK_F32) == "sweep2_kernel"
     assert _kernel_for("cube27", acc=_abi.BK_ACC_FLOATFLOAT) == "sweep_kernel"
+    # the 125-point cube's coefficients are mirror-symmetric: float-float on pair sums
+    assert _kernel_for("cube125", acc=_abi.BK_ACC_FLOATFLOAT) == "sweep2_kernel"
     assert _kernel_for("cond7") == "sweep_kernel"  # pointwise operations: one-shot kernel only
     assert _kernel_for("star7", lay=B.Layout((8, 8, 8), (1, 2, 2))) == "sweep_kernel"
     assert _kernel_for("star7", lay=B.Layout((4, 4, 4), (1, 4, 4))) == "sweep2_kernel"
