@@ -247,7 +247,8 @@ int bk_sweep_kernel(const bk_field *in, const bk_field *out, const bk_stencil *s
   static thread_local Taps tp;  // the coefficient analysis decides the symmetric-cube routes
   int s = plan_sweep(in, out, st, lay, acc, &plan, &tp, &L);
   if (s) return s;
-  *name = plan.tma ? "sweep_star_tma_kernel" : plan.v2 ? "sweep2_kernel" : "sweep_kernel";
+  *name = plan.tma ? (tma_row(plan) ? "sweep_star_row_kernel" : "sweep_star_tma_kernel")
+          : plan.v2 ? "sweep2_kernel" : "sweep_kernel";
   return BK_OK;
 }
 

@@ -15,8 +15,8 @@
 // Each region lands densely in its own 128-byte aligned slice of a stage buffer; a stage
 // holds NB bricks.  Persistent CTAs, warp-specialised:
 //   * the last warp is the producer: its lanes 0..7*NB-1 each own one (brick, region) pair;
-//     they load the brick list one group and the adjacency entry half a group ahead, and for
-//     each group wait until the consumers have released the stage (mbarrier "empty"), then
+//     they load brick-list entries eight groups and adjacency entries four groups ahead, and
+//     for each group wait until the consumers have released the stage (mbarrier "empty"), then
 //     post the stage's byte count and issue the copies (mbarrier "full");
 //   * the other warps are consumers: wait for "full", compute, arrive on "empty".  Every
 //     thread computes one (j, i) column of its brick: k taps from registers, i / j taps from
@@ -130,6 +130,146 @@ __device__ __forceinline__ bool bar_red_or(int id, int count, bool pred) {
   return r != 0;
 }
 
+// A producer lane's look-ahead over the brick list and the adjacency: the list entry of
+// iteration it + 2D and the adjacency entry of iteration it + D load at iteration it, so each
+// load has D iterations to arrive before it is used (one memory latency per iteration would
+// otherwise bound the producer).
+template <int D>
+struct EntryRing {
+  unsigned b[2 * D], v[D];
+  template <class LB, class LA>
+  __device__ __forceinline__ void init(long long g0, long long gstep, LB load_b, LA load_adj) {
+#pragma unroll
+    for (int d = 0; d < 2 * D; ++d) b[d] = load_b(g0 + d * gstep);
+#pragma unroll
+    for (int d = 0; d < D; ++d) v[d] = load_adj(b[d]);
+  }
+  // the entries of the current iteration are b[0], v[0]; move to the next one
+  template <class LB, class LA>
+  __device__ __forceinline__ void advance(long long g, long long gstep, LB load_b, LA load_adj) {
+    const unsigned nv = load_adj(b[D]);
+    const unsigned nb = load_b(g + 2 * D * gstep);
+#pragma unroll
+    for (int d = 0; d + 1 < D; ++d) v[d] = v[d + 1];
+    v[D - 1] = nv;
+#pragma unroll
+    for (int d = 0; d + 1 < 2 * D; ++d) b[d] = b[d + 1];
+    b[2 * D - 1] = nb;
+  }
+};
+constexpr int PRODUCER_LOOKAHEAD = 4;
+
+// One consumer thread's column (fixed j, i; every k plane) of a star stencil over staged
+// regions, stored to `ob` (plane stride BJ*BI).  Offsets are in elements from `buf`: cKL / cC /
+// cKH address plane 0 of the column in the k-lo face, the centre and the k-hi face (plane
+// stride BJ*BI); oi / oj address the i / j taps (index 2(d-1) is +d, 2(d-1)+1 is -d) with
+// plane strides si / sj.  Float-float accumulation reads the stage as float pairs.
+template <typename T, int BK, int BJ, int BI, int R, int ACC>
+__device__ __forceinline__ void star_column(const unsigned char *buf, const int cKL, const int cC, const int cKH,
+                                            const int (&oi)[2 * R], const int (&si)[2 * R], const int (&oj)[2 * R],
+                                            const int (&sj)[2 * R], T *ob, const Taps &tp) {
+  typedef typename Elem<T>::acc AT;
+  constexpr int PK = BJ * BI;
+  if constexpr (ACC == ACCM_FF) {
+    const float2 *f = reinterpret_cast<const float2 *>(buf);
+    float2 w[BK + 2 * R];
+#pragma unroll
+    for (int kk = 0; kk < R; ++kk) w[kk] = f[cKL + kk * PK];
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) w[R + kk] = f[cC + kk * PK];
+#pragma unroll
+    for (int kk = 0; kk < R; ++kk) w[R + BK + kk] = f[cKH + kk * PK];
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      FFAcc acc;
+      acc.first(tp.cf[0], tp.cl[0], w[k + R]);
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+        acc.add(tp.cf[t + 0], tp.cl[t + 0], f[oi[q] + k * si[q]]);
+        acc.add(tp.cf[t + 1], tp.cl[t + 1], f[oi[q + 1] + k * si[q + 1]]);
+        acc.add(tp.cf[t + 2], tp.cl[t + 2], f[oj[q] + k * sj[q]]);
+        acc.add(tp.cf[t + 3], tp.cl[t + 3], f[oj[q + 1] + k * sj[q + 1]]);
+        acc.add(tp.cf[t + 4], tp.cl[t + 4], w[k + R + d]);
+        acc.add(tp.cf[t + 5], tp.cl[t + 5], w[k + R - d]);
+        acc.renorm();
+      }
+      store_stream(ob + k * PK, acc.result());
+    }
+  } else {
+    const T *f = reinterpret_cast<const T *>(buf);
+    AT w[BK + 2 * R];
+#pragma unroll
+    for (int kk = 0; kk < R; ++kk) w[kk] = to_acc(f[cKL + kk * PK]);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) w[R + kk] = to_acc(f[cC + kk * PK]);
+#pragma unroll
+    for (int kk = 0; kk < R; ++kk) w[R + BK + kk] = to_acc(f[cKH + kk * PK]);
+    if constexpr (ACC == ACCM_NATIVE && sizeof(AT) == 4) {
+      // two k planes per packed FP32 multiply-add (FFMA2): per point the same operations in
+      // the same order as the scalar path below, so the results are identical
+      static_assert(BK % 2 == 0, "k planes in pairs");
+      auto cc = [&](int t) {
+        const float c = coef<float>(tp, t);
+        return make_float2(c, c);
+      };
+#pragma unroll
+      for (int k = 0; k < BK; k += 2) {
+        auto ld2 = [&](int o, int st) { return make_float2(to_acc(f[o + k * st]), to_acc(f[o + (k + 1) * st])); };
+        float2 v = __fmul2_rn(cc(0), make_float2(w[k + R], w[k + R + 1]));
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+          v = __ffma2_rn(cc(t + 0), ld2(oi[q], si[q]), v);
+          v = __ffma2_rn(cc(t + 1), ld2(oi[q + 1], si[q + 1]), v);
+          v = __ffma2_rn(cc(t + 2), ld2(oj[q], sj[q]), v);
+          v = __ffma2_rn(cc(t + 3), ld2(oj[q + 1], sj[q + 1]), v);
+          v = __ffma2_rn(cc(t + 4), make_float2(w[k + R + d], w[k + R + 1 + d]), v);
+          v = __ffma2_rn(cc(t + 5), make_float2(w[k + R - d], w[k + R + 1 - d]), v);
+        }
+        store_stream(ob + k * PK, v.x);
+        store_stream(ob + (k + 1) * PK, v.y);
+      }
+    } else
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      AT v;
+      if constexpr (ACC == ACCM_NATIVE) {
+        v = coef<AT>(tp, 0) * w[k + R];
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+          v = fma(coef<AT>(tp, t + 0), to_acc(f[oi[q] + k * si[q]]), v);
+          v = fma(coef<AT>(tp, t + 1), to_acc(f[oi[q + 1] + k * si[q + 1]]), v);
+          v = fma(coef<AT>(tp, t + 2), to_acc(f[oj[q] + k * sj[q]]), v);
+          v = fma(coef<AT>(tp, t + 3), to_acc(f[oj[q + 1] + k * sj[q + 1]]), v);
+          v = fma(coef<AT>(tp, t + 4), w[k + R + d], v);
+          v = fma(coef<AT>(tp, t + 5), w[k + R - d], v);
+        }
+      } else {
+        AT row = coef<AT>(tp, 0) * w[k + R];
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+          row = fma(coef<AT>(tp, t + 0), to_acc(f[oi[q] + k * si[q]]), row);
+          row = fma(coef<AT>(tp, t + 1), to_acc(f[oi[q + 1] + k * si[q + 1]]), row);
+        }
+        AT s = row, comp = AT(0);
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+          neumaier(s, comp, coef<AT>(tp, t + 2) * to_acc(f[oj[q] + k * sj[q]]));
+          neumaier(s, comp, coef<AT>(tp, t + 3) * to_acc(f[oj[q + 1] + k * sj[q + 1]]));
+          neumaier(s, comp, coef<AT>(tp, t + 4) * w[k + R + d]);
+          neumaier(s, comp, coef<AT>(tp, t + 5) * w[k + R - d]);
+        }
+        v = s + comp;
+      }
+      store_stream(ob + k * PK, v);
+    }
+  }
+}
+
 template <typename T, int BK, int BJ, int BI, int R, int ACC, bool NI>
 __global__ void __launch_bounds__(StarTmaCfg<T, BK, BJ, BI, R, NI>::NT)
 sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp, const int S) {
@@ -195,9 +335,8 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     };
     unsigned pf = load_pf(g0 + PF * gstep);
     const char *in_bytes = reinterpret_cast<const char *>(a.in) + a.in_off * C::ES;
-    unsigned bq = load_b(g0);             // group of iteration it
-    unsigned vq = load_adj(bq);
-    unsigned bn = load_b(g0 + gstep);     // group of iteration it+1
+    EntryRing<PRODUCER_LOOKAHEAD> ring;
+    ring.init(g0, gstep, load_b, load_adj);
     int it = 0, st = 0;
     unsigned ph = 0;  // (it / S) & 1
     for (long long g = g0; g < ngroups; g += gstep, ++it) {
@@ -209,8 +348,9 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
         break;
       }
       if (__any_sync(0xFFFFFFFFu, *abort_word != 0)) break;
-      // checks of the entries loaded one iteration ago
-      unsigned v = vq;
+      // checks of this group's entries
+      const unsigned bq = ring.b[0];
+      unsigned v = ring.v[0];
       int act = 0;
       if (prod && bq != 0xFFFFFFFFu) {
         if (bq >= a.nbricks) {
@@ -236,9 +376,7 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
         else tma_load_3d(sbase + (st * NB + pbs) * C::BRICK + poff, &maps.m[pmap], px, py, (int)v, bar);
       }
       // advance the prefetch pipeline
-      bq = bn;
-      vq = load_adj(bn);
-      bn = load_b(g + 2 * gstep);
+      ring.advance(g, gstep, load_b, load_adj);
       if (++st == S) {
         st = 0;
         ph ^= 1u;
@@ -303,104 +441,8 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     }
     if (active) {
       T *ob = reinterpret_cast<T *>(a.out) + a.out_off + (size_t)ob_idx * a.out_step + (size_t)(j * BI + i);
-      if constexpr (ACC == ACCM_FF) {
-        const float2 *f = reinterpret_cast<const float2 *>(buf);
-        float2 w[BK + 2 * R];
-#pragma unroll
-        for (int kk = 0; kk < R; ++kk) w[kk] = f[eKL + (kk * BJ + j) * BI + i];
-#pragma unroll
-        for (int kk = 0; kk < BK; ++kk) w[R + kk] = f[eC + (kk * BJ + j) * BI + i];
-#pragma unroll
-        for (int kk = 0; kk < R; ++kk) w[R + BK + kk] = f[eKH + (kk * BJ + j) * BI + i];
-#pragma unroll
-        for (int k = 0; k < BK; ++k) {
-          FFAcc acc;
-          acc.first(tp.cf[0], tp.cl[0], w[k + R]);
-#pragma unroll
-          for (int d = 1; d <= R; ++d) {
-            const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
-            acc.add(tp.cf[t + 0], tp.cl[t + 0], f[oi[q] + k * si[q]]);
-            acc.add(tp.cf[t + 1], tp.cl[t + 1], f[oi[q + 1] + k * si[q + 1]]);
-            acc.add(tp.cf[t + 2], tp.cl[t + 2], f[oj[q] + k * sj[q]]);
-            acc.add(tp.cf[t + 3], tp.cl[t + 3], f[oj[q + 1] + k * sj[q + 1]]);
-            acc.add(tp.cf[t + 4], tp.cl[t + 4], w[k + R + d]);
-            acc.add(tp.cf[t + 5], tp.cl[t + 5], w[k + R - d]);
-            acc.renorm();
-          }
-          store_stream(ob + k * PK, acc.result());
-        }
-      } else {
-        const T *f = reinterpret_cast<const T *>(buf);
-        AT w[BK + 2 * R];
-#pragma unroll
-        for (int kk = 0; kk < R; ++kk) w[kk] = to_acc(f[eKL + (kk * BJ + j) * BI + i]);
-#pragma unroll
-        for (int kk = 0; kk < BK; ++kk) w[R + kk] = to_acc(f[eC + (kk * BJ + j) * BI + i]);
-#pragma unroll
-        for (int kk = 0; kk < R; ++kk) w[R + BK + kk] = to_acc(f[eKH + (kk * BJ + j) * BI + i]);
-        if constexpr (ACC == ACCM_NATIVE && sizeof(AT) == 4) {
-          // two k planes per packed FP32 multiply-add (FFMA2): per point the same operations in
-          // the same order as the scalar path below, so the results are identical
-          static_assert(BK % 2 == 0, "k planes in pairs");
-          auto cc = [&](int t) {
-            const float c = coef<float>(tp, t);
-            return make_float2(c, c);
-          };
-#pragma unroll
-          for (int k = 0; k < BK; k += 2) {
-            auto ld2 = [&](int o, int st) { return make_float2(to_acc(f[o + k * st]), to_acc(f[o + (k + 1) * st])); };
-            float2 v = __fmul2_rn(cc(0), make_float2(w[k + R], w[k + R + 1]));
-#pragma unroll
-            for (int d = 1; d <= R; ++d) {
-              const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
-              v = __ffma2_rn(cc(t + 0), ld2(oi[q], si[q]), v);
-              v = __ffma2_rn(cc(t + 1), ld2(oi[q + 1], si[q + 1]), v);
-              v = __ffma2_rn(cc(t + 2), ld2(oj[q], sj[q]), v);
-              v = __ffma2_rn(cc(t + 3), ld2(oj[q + 1], sj[q + 1]), v);
-              v = __ffma2_rn(cc(t + 4), make_float2(w[k + R + d], w[k + R + 1 + d]), v);
-              v = __ffma2_rn(cc(t + 5), make_float2(w[k + R - d], w[k + R + 1 - d]), v);
-            }
-            store_stream(ob + k * PK, v.x);
-            store_stream(ob + (k + 1) * PK, v.y);
-          }
-        } else
-#pragma unroll
-        for (int k = 0; k < BK; ++k) {
-          AT v;
-          if constexpr (ACC == ACCM_NATIVE) {
-            v = coef<AT>(tp, 0) * w[k + R];
-#pragma unroll
-            for (int d = 1; d <= R; ++d) {
-              const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
-              v = fma(coef<AT>(tp, t + 0), to_acc(f[oi[q] + k * si[q]]), v);
-              v = fma(coef<AT>(tp, t + 1), to_acc(f[oi[q + 1] + k * si[q + 1]]), v);
-              v = fma(coef<AT>(tp, t + 2), to_acc(f[oj[q] + k * sj[q]]), v);
-              v = fma(coef<AT>(tp, t + 3), to_acc(f[oj[q + 1] + k * sj[q + 1]]), v);
-              v = fma(coef<AT>(tp, t + 4), w[k + R + d], v);
-              v = fma(coef<AT>(tp, t + 5), w[k + R - d], v);
-            }
-          } else {
-            AT row = coef<AT>(tp, 0) * w[k + R];
-#pragma unroll
-            for (int d = 1; d <= R; ++d) {
-              const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
-              row = fma(coef<AT>(tp, t + 0), to_acc(f[oi[q] + k * si[q]]), row);
-              row = fma(coef<AT>(tp, t + 1), to_acc(f[oi[q + 1] + k * si[q + 1]]), row);
-            }
-            AT s = row, comp = AT(0);
-#pragma unroll
-            for (int d = 1; d <= R; ++d) {
-              const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
-              neumaier(s, comp, coef<AT>(tp, t + 2) * to_acc(f[oj[q] + k * sj[q]]));
-              neumaier(s, comp, coef<AT>(tp, t + 3) * to_acc(f[oj[q + 1] + k * sj[q + 1]]));
-              neumaier(s, comp, coef<AT>(tp, t + 4) * w[k + R + d]);
-              neumaier(s, comp, coef<AT>(tp, t + 5) * w[k + R - d]);
-            }
-            v = s + comp;
-          }
-          store_stream(ob + k * PK, v);
-        }
-      }
+      star_column<T, BK, BJ, BI, R, ACC>(buf, eKL + j * BI + i, eC + j * BI + i, eKH + j * BI + i, oi, si, oj, sj, ob,
+                                         tp);
     }
     // the float-float conversion wrote the stage through the generic proxy; order those
     // writes before the copies that refill it

@@ -469,5 +469,8 @@ int sweep_dispatch_f32(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStr
 int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
 int sweep_dispatch_tma(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s);
 bool tma_eligible(const SweepPlan &p, const bk_field *in);
+// Whether a TMA sweep takes the row-run kernel (2- and 4-byte storage; BK_TMA_ROW=0 selects
+// per-brick staging).
+bool tma_row(const SweepPlan &p);
 
 }  // namespace bk

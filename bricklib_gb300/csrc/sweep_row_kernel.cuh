@@ -1,0 +1,389 @@
+// Star-stencil brick sweep over runs of i-adjacent bricks, fed by the Tensor Memory
+// Accelerator (2- and 4-byte storage, row-major 8x8x8 bricks).
+//
+// A brick list in grid order is made of rows of bricks that are neighbours along i (the
+// reference's drivers sweep bricks in that order).  The kernel takes the list in segments of
+// NB entries and splits every segment into runs: maximal stretches of entries where entry n+1
+// is entry n's i-hi neighbour (adjacency slot 14) and entry n is entry n+1's i-lo neighbour
+// (slot 12).  One pipeline stage holds one run of L bricks:
+//   slots 0 .. L+1  whole bricks: the run's i-lo neighbour, the L centre bricks, the run's
+//                   i-hi neighbour (box (BJ*BI, BK) of the 3-D view (j*BI + i, k, brick));
+//   face block n    brick n's k faces (box (BJ*BI, R)) and j faces (box (R*BI, BK)).
+// Brick n's i taps read the slots either side of its own, so a run loads L + 2 whole bricks
+// where per-brick staging loads 3 L.  A list that is not in grid order runs as runs of one
+// brick.  Persistent CTAs, warp-specialised like the per-brick kernel: the last warp produces
+// (lanes 0 .. 7*NB-1 each own one (entry, region) pair of the segment; list and adjacency
+// entries load several segments ahead), the other warps consume (brick slot n+1 belongs to
+// consumer warp n, whose lanes compute one (j, i, i+1) column pair each).  The number of
+// stages a segment takes is known only to the producer, so it ends the stream with a marker
+// stage that carries no copies.  Every wait is bounded (about a second), after which the CTA
+// sets a device error flag and stops.  Summation order is that of the pipelined kernel.
+#pragma once
+
+#include "sweep3_kernel.cuh"
+
+namespace bk {
+
+template <typename T, int R>
+struct RowTmaCfg {
+  static constexpr int BK = 8, BJ = 8, BI = 8, PK = BJ * BI;
+  static constexpr int ES = (int)sizeof(T);
+  static constexpr int NB = 4;           // list entries per segment, bricks per stage at most
+  static constexpr int NC = NB * 32;     // consumer threads: one warp per brick slot
+  static constexpr int NT = NC + 32;     // + the producer warp
+  static constexpr int al(int b) { return (b + 127) / 128 * 128; }
+  static constexpr int B_C = BK * BJ * BI * ES, B_KF = R * BJ * BI * ES, B_JF = BK * R * BI * ES;
+  static constexpr int PC = al(B_C);     // pitch of the whole-brick slots
+  static constexpr int O_KL = 0, O_KH = al(B_KF), O_JL = 2 * al(B_KF), O_JH = O_JL + al(B_JF);
+  static constexpr int PF = O_JH + al(B_JF);         // pitch of the face blocks
+  static constexpr int FACES = (NB + 2) * PC;        // face blocks after the slots
+  static constexpr int STAGE = FACES + NB * PF;      // bytes of one stage
+  static constexpr int TXB = B_C + 2 * (B_KF + B_JF);  // bytes one run brick brings
+  // after the stages: full[4], empty[4] mbarriers, centre brick index [4][NB], abort word
+  static constexpr int META = 64 + 4 * TMA_MAX_STAGES * NB + 16;
+  static constexpr int smem(int stages) { return 128 + stages * STAGE + META; }
+};
+
+// Two adjacent elements (i, i+1) of a brick row in FP32: one 8-byte (FP32) or 4-byte (BF16)
+// shared-memory load, one store of the same width.  bf16 -> fp32 is exact (the bf16 bits are
+// the high half of the fp32 word); fp32 -> bf16 rounds to nearest even as the scalar path.
+__device__ __forceinline__ float2 ld_pair(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ float2 ld_pair(const __nv_bfloat16 *p) {
+  const unsigned u = *reinterpret_cast<const unsigned *>(p);
+  return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xFFFF0000u));
+}
+__device__ __forceinline__ void st_pair(float *p, float2 v) { __stcs(reinterpret_cast<float2 *>(p), v); }
+__device__ __forceinline__ void st_pair(__nv_bfloat16 *p, float2 v) {
+  *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(v.x, v.y);
+}
+
+// Element offsets (from the stage base, plane 0) of one thread's taps for columns (i0, i0+1):
+// a[m + MI] = the aligned pair (i0 + 2m, i0 + 2m + 1), m = -MI..MI, MI = ceil(R/2) (m = 0 is the
+// centre; the others may sit in the slots either side); oj / sj the j taps (index 2(d-1) is +d,
+// 2(d-1)+1 is -d) and their plane strides; kl / kh plane 0 of the k faces.
+template <int R>
+struct RowPairTaps {
+  int a[2 * ((R + 1) / 2) + 1];
+  int oj[2 * R], sj[2 * R];
+  int kl, kh;
+};
+
+// Columns (i0, i0+1) of a star stencil over every k plane, with FP32 arithmetic: packed FFMA2
+// on the column pair (native), or scalar compensated sums per column.  Per point the terms and
+// their order are those of the per-brick kernels: centre, then for d = 1..R: i+d, i-d, j+d,
+// j-d, k+d, k-d; a pair tap at odd distance d joins the halves of two aligned pairs.
+template <typename T, int R, int ACC>
+__device__ __forceinline__ void star_pair_column(const T *f, const RowPairTaps<R> &o, T *ob, const Taps &tp) {
+  constexpr int BK = 8, PK = 64, MI = (R + 1) / 2;
+  float2 w[BK + 2 * R];
+#pragma unroll
+  for (int kk = 0; kk < R; ++kk) w[kk] = ld_pair(f + o.kl + kk * PK);
+#pragma unroll
+  for (int kk = 0; kk < BK; ++kk) w[R + kk] = ld_pair(f + o.a[MI] + kk * PK);
+#pragma unroll
+  for (int kk = 0; kk < R; ++kk) w[R + BK + kk] = ld_pair(f + o.kh + kk * PK);
+#pragma unroll
+  for (int k = 0; k < BK; ++k) {
+    float2 A[2 * MI + 1];
+#pragma unroll
+    for (int m = 0; m < 2 * MI + 1; ++m) A[m] = m == MI ? w[k + R] : ld_pair(f + o.a[m] + k * PK);
+    auto ip = [&](int d) {  // taps (i0 + d, i0 + 1 + d)
+      return (d & 1) ? make_float2(A[MI + (d - 1) / 2].y, A[MI + (d + 1) / 2].x) : A[MI + d / 2];
+    };
+    auto im = [&](int d) {  // taps (i0 - d, i0 + 1 - d)
+      return (d & 1) ? make_float2(A[MI - (d + 1) / 2].y, A[MI - (d - 1) / 2].x) : A[MI - d / 2];
+    };
+    auto jt = [&](int q) { return ld_pair(f + o.oj[q] + k * o.sj[q]); };
+    float2 v;
+    if constexpr (ACC == ACCM_NATIVE) {
+      auto cc = [&](int t) {
+        const float c = coef<float>(tp, t);
+        return make_float2(c, c);
+      };
+      v = __fmul2_rn(cc(0), w[k + R]);
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+        v = __ffma2_rn(cc(t + 0), ip(d), v);
+        v = __ffma2_rn(cc(t + 1), im(d), v);
+        v = __ffma2_rn(cc(t + 2), jt(q), v);
+        v = __ffma2_rn(cc(t + 3), jt(q + 1), v);
+        v = __ffma2_rn(cc(t + 4), w[k + R + d], v);
+        v = __ffma2_rn(cc(t + 5), w[k + R - d], v);
+      }
+    } else {
+      float2 row;
+      row.x = coef<float>(tp, 0) * w[k + R].x;
+      row.y = coef<float>(tp, 0) * w[k + R].y;
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1);
+        const float2 p = ip(d), m = im(d);
+        row.x = fmaf(coef<float>(tp, t + 0), p.x, row.x);
+        row.y = fmaf(coef<float>(tp, t + 0), p.y, row.y);
+        row.x = fmaf(coef<float>(tp, t + 1), m.x, row.x);
+        row.y = fmaf(coef<float>(tp, t + 1), m.y, row.y);
+      }
+      float2 acc = row, comp = make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+        const float2 jp = jt(q), jm = jt(q + 1);
+        neumaier(acc.x, comp.x, coef<float>(tp, t + 2) * jp.x);
+        neumaier(acc.y, comp.y, coef<float>(tp, t + 2) * jp.y);
+        neumaier(acc.x, comp.x, coef<float>(tp, t + 3) * jm.x);
+        neumaier(acc.y, comp.y, coef<float>(tp, t + 3) * jm.y);
+        neumaier(acc.x, comp.x, coef<float>(tp, t + 4) * w[k + R + d].x);
+        neumaier(acc.y, comp.y, coef<float>(tp, t + 4) * w[k + R + d].y);
+        neumaier(acc.x, comp.x, coef<float>(tp, t + 5) * w[k + R - d].x);
+        neumaier(acc.y, comp.y, coef<float>(tp, t + 5) * w[k + R - d].y);
+      }
+      v = make_float2(acc.x + comp.x, acc.y + comp.y);
+    }
+    st_pair(ob + k * PK, v);
+  }
+}
+
+template <typename T, int R, int ACC>
+__global__ void __launch_bounds__(RowTmaCfg<T, R>::NT)
+sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp, const int S) {
+  typedef RowTmaCfg<T, R> C;
+  constexpr int NB = C::NB, BK = C::BK, BJ = C::BJ, BI = C::BI, PK = C::PK, E = C::ES;
+  constexpr unsigned NONE = 0xFFFFFFFFu;  // slot without a brick in this stage
+  constexpr unsigned END = 0xFFFFFFFEu;   // no further stages
+  constexpr unsigned ALL = 0xFFFFFFFFu;
+  static_assert(7 * NB <= 28, "one producer lane per (entry, region), four prefetch lanes");
+  static_assert(E <= 4, "2- and 4-byte storage");
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const unsigned raw = smem_u32(smem_raw);
+  const unsigned pad = (128u - (raw & 127u)) & 127u;
+  unsigned char *sm = smem_raw + pad;  // 128-byte aligned stages
+  const unsigned sbase = raw + pad;
+  const unsigned full0 = sbase + S * C::STAGE, empty0 = full0 + 8 * TMA_MAX_STAGES;
+  unsigned *outb = reinterpret_cast<unsigned *>(sm + S * C::STAGE + 64);  // [S][NB]
+  volatile int *abort_word = reinterpret_cast<volatile int *>(sm + S * C::STAGE + 64 + 4 * TMA_MAX_STAGES * NB);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, C::NC / 32);
+    }
+    *abort_word = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+
+  const long long nseg = ((long long)a.nlist + NB - 1) / NB;
+  const long long g0 = blockIdx.x, gstep = gridDim.x;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x >= C::NC) {
+    // ------------------------------------------------------------------ producer warp
+    const bool prod = lane < 7 * NB;
+    const int pbs = lane / 7, prg = lane - (lane / 7) * 7;  // segment entry, region
+    // region prg: 0 centre, 1 k-lo, 2 k-hi, 3 j-lo, 4 j-hi, 5 i-lo, 6 i-hi
+    const int pslot = prg == 0 ? 13 : prg == 1 ? 4 : prg == 2 ? 22 : prg == 3 ? 10 : prg == 4 ? 16 : prg == 5 ? 12 : 14;
+    const int pmap = prg == 1 || prg == 2 ? 1 : prg == 3 || prg == 4 ? 2 : 0;
+    const int px = prg == 3 ? (BJ - R) * BI : 0, py = prg == 1 ? BK - R : 0;
+    const int poff = prg == 1 ? C::O_KL : prg == 2 ? C::O_KH : prg == 3 ? C::O_JL : C::O_JH;  // faces only
+    auto load_b = [&](long long grp) -> unsigned {
+      const long long n = grp * NB + pbs;
+      return (prod && grp < nseg && n < (long long)a.nlist) ? a.blist[n] : NONE;
+    };
+    auto load_adj = [&](unsigned b) -> unsigned {
+      return (prod && b < a.nbricks) ? a.adj[(size_t)b * 27 + pslot] : 0u;
+    };
+    // lanes 28..31 prefetch the centre bricks of the segment PF iterations ahead into L2
+    constexpr int PF = 2;
+    const bool pfl = lane >= 7 * NB && lane < 8 * NB;
+    const int pfs = lane - 7 * NB;
+    auto load_pf = [&](long long grp) -> unsigned {
+      const long long n = grp * NB + pfs;
+      return (pfl && grp < nseg && n < (long long)a.nlist) ? a.blist[n] : NONE;
+    };
+    unsigned pf = load_pf(g0 + PF * gstep);
+    const char *in_bytes = reinterpret_cast<const char *>(a.in) + a.in_off * E;
+    EntryRing<PRODUCER_LOOKAHEAD> ring;
+    ring.init(g0, gstep, load_b, load_adj);
+    int it = 0, st = 0;                // stages issued, current stage
+    unsigned ph = 0;                   // (it / S) & 1
+    bool stop = false;
+    for (long long g = g0; g < nseg && !stop; g += gstep) {
+      // checks of this segment's entries: out-of-range faces read brick 0, an entry whose
+      // brick or centre is out of range is skipped; both raise the bounds flag
+      const unsigned bq = ring.b[0];
+      unsigned v = ring.v[0];
+      int act = 0;
+      if (prod && bq != NONE) {
+        if (bq >= a.nbricks) {
+          if (prg == 0) atomicOr(a.err, FLAG_BOUNDS);
+        } else {
+          act = prg != 0 || ((long long)v < a.out_chunks && (long long)v < a.in_chunks);
+          if ((long long)v >= a.in_chunks || !act) {
+            atomicOr(a.err, FLAG_BOUNDS);
+            v = 0;
+          }
+        }
+      }
+      // entries that run (bit n), and entries n, n+1 that are i-neighbours of each other (bit n)
+      const unsigned am = __ballot_sync(ALL, prod && prg == 0 && act);
+      const unsigned vn = __shfl_down_sync(ALL, v, 1);   // lane 7n+6 <- centre of entry n+1
+      const unsigned vp = __shfl_up_sync(ALL, v, 12);    // lane 7(n+1)+5 <- centre of entry n
+      const unsigned c1 = __ballot_sync(ALL, prod && prg == 6 && pbs + 1 < NB && v == vn);
+      const unsigned c2 = __ballot_sync(ALL, prod && prg == 5 && pbs >= 1 && v == vp);
+      unsigned bm = 0, cm = 0;
+#pragma unroll
+      for (int n = 0; n < NB; ++n) {
+        if ((am >> (7 * n)) & 1u) bm |= 1u << n;
+        if (n + 1 < NB && ((c1 >> (7 * n + 6)) & 1u) && ((c2 >> (7 * n + 12)) & 1u)) cm |= 1u << n;
+      }
+      ring.advance(g, gstep, load_b, load_adj);
+      unsigned todo = bm;
+      while (todo) {  // one stage per run; warp-uniform
+        const int s0 = __ffs(todo) - 1;
+        int e = s0 + 1;
+        while (e < NB && ((todo >> e) & 1u) && ((cm >> (e - 1)) & 1u)) ++e;
+        todo &= ~((1u << e) - 1u);
+        const bool freed = it < S || mbar_wait_bounded(empty0 + 8 * st, ph ^ 1u);
+        if (!__all_sync(ALL, freed)) {
+          if (lane == 0) atomicOr(a.err, FLAG_TIMEOUT);
+          *abort_word = 1;
+          stop = true;
+          break;
+        }
+        if (__any_sync(ALL, *abort_word != 0)) {
+          stop = true;
+          break;
+        }
+        const int L = e - s0;
+        const int src = s0 + lane < NB ? s0 + lane : NB - 1;
+        const unsigned cv = __shfl_sync(ALL, v, 7 * src);
+        if (lane < NB) outb[st * NB + lane] = lane < L ? cv : NONE;
+        __syncwarp();  // the centre indices are written before the phase can complete
+        const unsigned bar = full0 + 8 * st;
+        if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)(L * C::TXB + 2 * C::B_C));
+        __syncwarp();
+        if (prod && pbs >= s0 && pbs < e) {
+          const unsigned stage = sbase + st * C::STAGE;
+          const int slot = pbs - s0 + 1;
+          if (prg == 0) tma_load_3d(stage + slot * C::PC, &maps.m[0], 0, 0, (int)v, bar);
+          else if (prg == 5) {
+            if (pbs == s0) tma_load_3d(stage, &maps.m[0], 0, 0, (int)v, bar);
+          } else if (prg == 6) {
+            if (pbs == e - 1) tma_load_3d(stage + (L + 1) * C::PC, &maps.m[0], 0, 0, (int)v, bar);
+          } else {
+            tma_load_3d(stage + C::FACES + (slot - 1) * C::PF + poff, &maps.m[pmap], px, py, (int)v, bar);
+          }
+        }
+        ++it;
+        if (++st == S) {
+          st = 0;
+          ph ^= 1u;
+        }
+      }
+      if (pfl && (long long)pf < a.in_chunks)
+        prefetch_l2(in_bytes + (size_t)pf * a.in_step * E, (unsigned)C::B_C);
+      pf = load_pf(g + (PF + 1) * gstep);
+    }
+    if (!stop) {
+      // the end marker: a stage whose phase completes without copies
+      const bool freed = it < S || mbar_wait_bounded(empty0 + 8 * st, ph ^ 1u);
+      if (__all_sync(ALL, freed)) {
+        if (lane < NB) outb[st * NB + lane] = END;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(full0 + 8 * st);
+        ++it;
+      } else {
+        if (lane == 0) atomicOr(a.err, FLAG_TIMEOUT);
+        *abort_word = 1;
+      }
+    }
+    // copies of the last S issued stages may still be in flight after an abort
+    if (lane == 0)
+      for (int q = it - S > 0 ? it - S : 0; q < it; ++q)
+        if (!mbar_wait_bounded(full0 + 8 * (q % S), (unsigned)(q / S) & 1u)) break;
+    return;
+  }
+
+  // -------------------------------------------------------------------- consumer warps
+  // one warp per brick slot; lane = (j, pair of i columns)
+  const int bs = threadIdx.x >> 5;
+  const int j = lane >> 2, i0 = 2 * (lane & 3);
+  const int slot = bs + 1;
+  constexpr int SE = C::PC / E;  // slot pitch in elements
+  constexpr int MI = (R + 1) / 2;
+  const int fb = (C::FACES + bs * C::PF) / E;
+  RowPairTaps<R> o;
+#pragma unroll
+  for (int m = -MI; m <= MI; ++m) {
+    const int c = i0 + 2 * m;
+    o.a[m + MI] = (c >= BI ? (slot + 1) * SE + (c - BI) : c < 0 ? (slot - 1) * SE + (c + BI) : slot * SE + c) + j * BI;
+  }
+#pragma unroll
+  for (int d = 1; d <= R; ++d) {
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+      const int q = 2 * (d - 1) + sg;
+      const int jj = sg ? j - d : j + d;
+      if (jj >= BJ) { o.oj[q] = fb + C::O_JH / E + (jj - BJ) * BI + i0; o.sj[q] = R * BI; }
+      else if (jj < 0) { o.oj[q] = fb + C::O_JL / E + (R + jj) * BI + i0; o.sj[q] = R * BI; }
+      else { o.oj[q] = slot * SE + jj * BI + i0; o.sj[q] = PK; }
+    }
+  }
+  o.kl = fb + C::O_KL / E + j * BI + i0;
+  o.kh = fb + C::O_KH / E + j * BI + i0;
+
+  int st = 0;
+  unsigned ph = 0;
+  for (;;) {
+    const bool ok = __all_sync(ALL, mbar_wait_bounded(full0 + 8 * st, ph));
+    if (!ok) {
+      atomicOr(a.err, FLAG_TIMEOUT);
+      *abort_word = 1;
+      break;
+    }
+    const unsigned ob_idx = outb[st * NB + bs];
+    if (ob_idx == END) break;
+    if (ob_idx != NONE) {
+      T *ob = reinterpret_cast<T *>(a.out) + a.out_off + (size_t)ob_idx * a.out_step + (size_t)(j * BI + i0);
+      star_pair_column<T, R, ACC>(reinterpret_cast<const T *>(sm + st * C::STAGE), o, ob, tp);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(empty0 + 8 * st);
+    if (++st == S) {
+      st = 0;
+      ph ^= 1u;
+    }
+  }
+}
+
+template <typename T, int R, int ACC>
+int launch_star_row(const SweepArgs &a, const Taps &tp, int dtype, cudaStream_t s) {
+  typedef RowTmaCfg<T, R> C;
+  const int S = tma_stages(2);
+  const int smem = C::smem(S);
+  if (smem > 227 * 1024) return fail(BK_ERR_UNSUPPORTED, "row TMA sweep stages exceed shared memory");
+  TmaMaps maps;
+  if (!star_tma_maps(a, dtype, C::BK, C::BJ, C::BI, R, C::BI, &maps))
+    return fail(BK_ERR_UNSUPPORTED, "field not describable to the TMA unit");
+  auto kern = sweep_star_row_kernel<T, R, ACC>;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, smem);
+  if (e != cudaSuccess) return cuda_fail(e, "row TMA sweep launch setup");
+  if (per_sm < 1) return fail(BK_ERR_UNSUPPORTED, "row TMA sweep does not fit on an SM");
+  const long long segs = ((long long)a.nlist + C::NB - 1) / C::NB;
+  long long grid = (long long)sms * per_sm;
+  if (grid > segs) grid = segs;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, C::NT, smem, s>>>(maps, a, tp, S);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "row TMA sweep launch");
+  return BK_OK;
+}
+
+}  // namespace bk

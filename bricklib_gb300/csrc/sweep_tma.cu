@@ -3,7 +3,7 @@
 #include <cstdlib>
 #include <cstring>
 
-#include "sweep3_kernel.cuh"
+#include "sweep_row_kernel.cuh"
 
 namespace bk {
 
@@ -77,11 +77,20 @@ static bool narrow_iface(int dtype) {
   return dtype == BK_F64;
 }
 
+bool tma_row(const SweepPlan &p) {
+  if (!p.tma || p.dtype == BK_F64 || p.acc == ACCM_FF) return false;
+  const char *e = getenv("BK_TMA_ROW");
+  return !(e && !strcmp(e, "0"));
+}
+
 #define BK_TMA_CASE(T_, R_, ACC_)                                                    \
   if (p.r == R_ && p.acc == ACC_)                                                   \
     return narrow_iface(p.dtype) ? launch_star_tma<T_, 8, 8, 8, R_, ACC_, true>(a, tp, p.dtype, s) \
                                  : launch_star_tma<T_, 8, 8, 8, R_, ACC_, false>(a, tp, p.dtype, s);
 #define BK_TMA_RADII(T_, ACC_) BK_TMA_CASE(T_, 1, ACC_) BK_TMA_CASE(T_, 2, ACC_) BK_TMA_CASE(T_, 4, ACC_)
+#define BK_ROW_CASE(T_, R_, ACC_) \
+  if (p.r == R_ && p.acc == ACC_) return launch_star_row<T_, R_, ACC_>(a, tp, p.dtype, s);
+#define BK_ROW_RADII(T_, ACC_) BK_ROW_CASE(T_, 1, ACC_) BK_ROW_CASE(T_, 2, ACC_) BK_ROW_CASE(T_, 4, ACC_)
 
 int sweep_dispatch_tma(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
   if (p.fam != FAM_STAR || p.shape != 0 || !p.rm)
@@ -92,10 +101,20 @@ int sweep_dispatch_tma(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStr
       BK_TMA_RADII(double, ACCM_FF)
       break;
     case BK_F32:
+      if (tma_row(p)) {
+        BK_ROW_RADII(float, ACCM_NATIVE)
+        BK_ROW_RADII(float, ACCM_COMP)
+        break;
+      }
       BK_TMA_RADII(float, ACCM_NATIVE)
       BK_TMA_RADII(float, ACCM_COMP)
       break;
     case BK_BF16:
+      if (tma_row(p)) {
+        BK_ROW_RADII(__nv_bfloat16, ACCM_NATIVE)
+        BK_ROW_RADII(__nv_bfloat16, ACCM_COMP)
+        break;
+      }
       BK_TMA_RADII(__nv_bfloat16, ACCM_NATIVE)
       BK_TMA_RADII(__nv_bfloat16, ACCM_COMP)
       break;

@@ -307,6 +307,109 @@ def test_tma_star_kernel_equals_pipelined(dtype, acc, name, monkeypatch):
         assert int(np.count_nonzero((written != 0xFF).any(axis=1))) == nout
 
 
+def _row_lists(dom, seed):
+    """Brick lists for the row-run kernel: grid order (full runs), a shuffle (runs of one),
+    grid-order pieces of 1..9 bricks in shuffled order (runs cut at every alignment),
+    repeated entries, and an odd-length tail."""
+    rng = np.random.default_rng(seed)
+    it = np.asarray(dom.interior, dtype=np.uint32)
+    cuts = np.cumsum(rng.integers(1, 10, size=len(it)))
+    pieces = np.split(it, cuts[cuts < len(it)])
+    order = rng.permutation(len(pieces))
+    lists = {
+        "grid": it,
+        "shuffled": rng.permutation(it),
+        "pieces": np.concatenate([pieces[k] for k in order]),
+        "repeats": np.repeat(it[:300], rng.integers(1, 3, size=300)),
+        "tail": it[5:5 + 4 * 37 + 3],
+    }
+    return {k: np.ascontiguousarray(v, dtype=np.uint32) for k, v in lists.items()}
+
+
+@pytest.mark.parametrize("dtype,acc", [(BK_F32, BK_ACC_NATIVE), (BK_F32, BK_ACC_COMPENSATED),
+                                       (BK_BF16, BK_ACC_NATIVE), (BK_BF16, BK_ACC_COMPENSATED)])
+@pytest.mark.parametrize("name", ["star7", "star13", "star25"])
+def test_row_kernel_equals_per_brick_staging(dtype, acc, name, monkeypatch):
+    """The row-run TMA kernel (runs of i-adjacent list entries share their whole-brick i
+    faces) writes exactly what per-brick TMA staging and the pipelined kernel write, for
+    lists in grid order, shuffled, in grid-order pieces, with repeats and with a ragged tail."""
+    st = stencils.make(name, 17)
+    dom = GridDomain((64, 128, 128), dtype=dtype)  # 4,096 interior bricks
+    arr = stencils.uniform(37, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    monkeypatch.delenv("BK_TMA_ROW", raising=False)
+    assert B.sweepKernel(dom.brick(0), dom.brick(1), st, acc) == "sweep_star_row_kernel"
+    for key, lst in _row_lists(dom, 3).items():
+        dl = B.BrickList(lst)
+        row = _sweep_with(None, monkeypatch, dom, st, acc, dl)
+        monkeypatch.setenv("BK_TMA_ROW", "0")
+        per_brick = _sweep_with(None, monkeypatch, dom, st, acc, dl)
+        monkeypatch.delenv("BK_TMA_ROW")
+        piped = _sweep_with("BK_SWEEP_PIPELINED", monkeypatch, dom, st, acc, dl)
+        np.testing.assert_array_equal(row.view(np.uint8), per_brick.view(np.uint8), err_msg=key)
+        np.testing.assert_array_equal(row.view(np.uint8), piped.view(np.uint8), err_msg=key)
+        written = row.view(np.uint8).reshape(dom.nbricks, dom.nfields, -1)[:, 1, :]
+        assert int(np.count_nonzero((written != 0xFF).any(axis=1))) == len(np.unique(lst)), key
+
+
+@pytest.mark.parametrize("dtype", [BK_F32, BK_BF16])
+def test_row_kernel_follows_asymmetric_adjacency(dtype, monkeypatch):
+    """Runs need both directions: entry n+1 is entry n's i-hi neighbour AND entry n is entry
+    n+1's i-lo neighbour.  With one direction broken (i-lo re-pointed elsewhere, or a brick
+    whose i-hi is itself, periodic one brick wide) the row kernel still reads exactly the
+    adjacency the per-brick kernels read."""
+    st = stencils.make("star13", 5)
+    dom = GridDomain((32, 64, 64), dtype=dtype, device=False)
+    adj = dom.bInfo.adj.copy()
+    rng = np.random.default_rng(9)
+    it = dom.interior
+    victims = rng.choice(it, size=len(it) // 5, replace=False)
+    adj[victims, 12] = rng.choice(it, size=len(victims))          # i-lo elsewhere
+    selfies = rng.choice(it, size=len(it) // 7, replace=False)
+    adj[selfies, 14] = selfies                                       # i-hi is the brick itself
+    adj[selfies[::2], 12] = selfies[::2]                             # ... and i-lo too for half
+    dom.bInfo = B.BrickInfo(dom.nbricks, adj)
+    arr = stencils.uniform(8, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.to_device()
+    lst = np.concatenate([it, np.repeat(selfies[:50], 2)]).astype(np.uint32)
+    dl = B.BrickList(lst)
+    monkeypatch.delenv("BK_TMA_ROW", raising=False)
+    row = _sweep_with(None, monkeypatch, dom, st, BK_ACC_NATIVE, dl)
+    piped = _sweep_with("BK_SWEEP_PIPELINED", monkeypatch, dom, st, BK_ACC_NATIVE, dl)
+    np.testing.assert_array_equal(row.view(np.uint8), piped.view(np.uint8))
+
+
+def test_row_kernel_bounds_are_flagged(monkeypatch):
+    """Out-of-range adjacency and list entries on the row kernel: the bricks that can run
+    equal the per-brick kernel's output, and the bounds flag is raised."""
+    st = stencils.make("star7", 2)
+    dom = GridDomain((32, 32, 64), dtype=BK_F32, device=False)
+    adj = dom.bInfo.adj.copy()
+    it = dom.interior
+    adj[it[3], 14] = dom.nbricks + 7
+    adj[it[10], 12] = dom.nbricks + 9
+    dom.bInfo = B.BrickInfo(dom.nbricks, adj)
+    arr = stencils.uniform(6, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.to_device()
+    lst = B.BrickList(np.concatenate([it[:20], [dom.nbricks + 3], it[20:]]).astype(np.uint32))
+    outs = []
+    for row in ("1", "0"):
+        monkeypatch.setenv("BK_TMA_ROW", row)
+        raw = dom.storage.host.view(np.uint8).reshape(dom.nbricks, dom.nfields, -1)
+        raw[:, 1, :] = 0xFF
+        dom.upload()
+        B.error_flags()
+        B.brickSweep(dom.brick(0), dom.brick(1), lst, st)
+        B.synchronize()
+        assert B.error_flags() & 1
+        dom.download()
+        outs.append(dom.storage.host.copy())
+    np.testing.assert_array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
+
+
 @pytest.mark.parametrize("name,acc", [("star7", BK_ACC_NATIVE), ("cube27", BK_ACC_NATIVE),
                                       ("cube125", _abi.BK_ACC_FLOATFLOAT)])
 def test_output_field_in_mapped_host_memory(name, acc, kernel):

@@ -67,9 +67,15 @@ def _kernel_for(name, lay=None, dtype=_abi.BK_F64, acc=_abi.BK_ACC_NATIVE, offse
 def test_kernel_choice(monkeypatch):
     monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
     monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
+    monkeypatch.delenv("BK_TMA_ROW", raising=False)
     for name in ("star7", "star13", "star25", "heat7"):
-        for dt in (_abi.BK_F64, _abi.BK_F32, _abi.BK_BF16):
-            assert _kernel_for(name, dtype=dt) == "sweep_star_tma_kernel", (name, dt)
+        assert _kernel_for(name) == "sweep_star_tma_kernel", name
+        for dt in (_abi.BK_F32, _abi.BK_BF16):
+            assert _kernel_for(name, dtype=dt) == "sweep_star_row_kernel", (name, dt)
+            assert _kernel_for(name, dtype=dt, acc=_abi.BK_ACC_COMPENSATED) == "sweep_star_row_kernel", (name, dt)
+    monkeypatch.setenv("BK_TMA_ROW", "0")
+    assert _kernel_for("star7", dtype=_abi.BK_F32) == "sweep_star_tma_kernel"
+    monkeypatch.delenv("BK_TMA_ROW")
     assert _kernel_for("star7", acc=_abi.BK_ACC_FLOATFLOAT) == "sweep_star_tma_kernel"
     assert _kernel_for("cube27") == "sweep2_kernel"
     assert _kernel_for("cube125", dtype=_abi.BK_F32) == "sweep2_kernel"
