@@ -126,6 +126,7 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
       plan->symij = ij;
     }
   }
+  for (int t = 0; t < TAP_PAIRS; ++t) tp->cp[t] = make_float2(tp->cf[t], tp->cf[t]);
   return BK_OK;
 }
 

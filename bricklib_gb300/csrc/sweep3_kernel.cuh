@@ -209,10 +209,8 @@ __device__ __forceinline__ void star_column(const unsigned char *buf, const int 
       // two k planes per packed FP32 multiply-add (FFMA2): per point the same operations in
       // the same order as the scalar path below, so the results are identical
       static_assert(BK % 2 == 0, "k planes in pairs");
-      auto cc = [&](int t) {
-        const float c = coef<float>(tp, t);
-        return make_float2(c, c);
-      };
+      auto cc = [&](int t) { return tp.cp[t]; };
+      static_assert(1 + 6 * R <= TAP_PAIRS, "coefficient pairs");
 #pragma unroll
       for (int k = 0; k < BK; k += 2) {
         auto ld2 = [&](int o, int st) { return make_float2(to_acc(f[o + k * st]), to_acc(f[o + (k + 1) * st])); };

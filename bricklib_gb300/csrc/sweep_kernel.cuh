@@ -60,6 +60,9 @@ struct SweepArgs {
   int parity;
 };
 
+// Taps with a packed-FP32 coefficient pair (every star up to radius 5).
+constexpr int TAP_PAIRS = 32;
+
 // Coefficients in kernel order; passed by value (kernel parameter constant bank).
 struct Taps {
   int n;
@@ -68,6 +71,7 @@ struct Taps {
   float cf[BK_MAX_TAPS];   // coefficient rounded to float (the high part)
   float cl[BK_MAX_TAPS];   // float(c - cf): the low part, for float-float arithmetic
   double c[BK_MAX_TAPS];
+  float2 cp[TAP_PAIRS];    // (cf, cf) of the first taps: operands of packed FP32 arithmetic
 };
 
 __host__ __device__ constexpr int sweep_threads(int tpb) { return tpb < 128 ? 128 : tpb; }

@@ -96,10 +96,8 @@ __device__ __forceinline__ void star_pair_column(const T *f, const RowPairTaps<R
     auto jt = [&](int q) { return ld_pair(f + o.oj[q] + k * o.sj[q]); };
     float2 v;
     if constexpr (ACC == ACCM_NATIVE) {
-      auto cc = [&](int t) {
-        const float c = coef<float>(tp, t);
-        return make_float2(c, c);
-      };
+      auto cc = [&](int t) { return tp.cp[t]; };
+      static_assert(1 + 6 * R <= TAP_PAIRS, "coefficient pairs");
       v = __fmul2_rn(cc(0), w[k + R]);
 #pragma unroll
       for (int d = 1; d <= R; ++d) {
