@@ -345,6 +345,16 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
         e_ms = max_over_ranks(e0.elapsed_time(e1) / Ke)
+        # the link rates this box gives alone (after the timed region): one copy each way
+        link = {}
+        for key, dst, src, kind in (("h2d_gbs", s_in2.ptr, h_in.ptr, 0),
+                                    ("d2h_gbs", h_in.ptr, s_out2.ptr, 1)):
+            la, lb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            la.record(stream)
+            B.memcpy(dst, src, nbytes, kind, sp)
+            lb.record(stream)
+            torch.cuda.synchronize()
+            link[key] = round(nbytes / (la.elapsed_time(lb) * 1e-3) / 1e9, 1)
         # every host result equals the device sweep's
         dev_out = np.empty(nbricks * bsize, dtype=B.NP_DTYPE[dtype])
         for name in shapes:
@@ -355,6 +365,7 @@ def run_ours(args):
                 raise RuntimeError(f"{name}: the result in host memory differs from the device sweep")
         e2e = {"value": round(ws * len(shapes) * points / (e_ms * 1e-3) / 1e9, 3), "unit": "GStencil/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3),
+               "link_alone": link,
                "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a copy "
                        "stream under the previous step's sweeps; results: device-to-host copies on a second "
                        "stream under the next sweep, the last sweep storing straight into mapped page-locked "

@@ -154,18 +154,20 @@ int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, in
  *              grid[GB..STRIDEB-GB)^3 of 3axis.cu:167)
  * Neighbour or list indices >= chunks/nbricks are clamped to brick 0 and reported by
  * bk_error_flags() as BK_ERR_BOUNDS; the kernel never reads outside the storage.
- * Three kernels implement it: a TMA-fed one (7/13/25-point stars on row-major 8x8x8
- * bricks, 16-byte aligned input), a pipelined one (row-major layouts, 16-byte aligned
- * input) and a one-shot one (everything).  The environment variables BK_SWEEP_ONESHOT=1
- * and BK_SWEEP_PIPELINED=1 override the built-in choice (used by the parity tests);
- * BK_TMA_STAGES (2..4) and BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernel. */
+ * Four kernels implement it: two TMA-fed ones for 7/13/25-point stars on row-major 8x8x8
+ * bricks with 16-byte aligned input (FP32 / BF16: runs of i-adjacent list entries share
+ * their i-neighbour bricks; FP64: per-brick staging), a pipelined one (row-major layouts,
+ * 16-byte aligned input) and a one-shot one (everything).  The environment variables
+ * BK_SWEEP_ONESHOT=1 and BK_SWEEP_PIPELINED=1 override the built-in choice (used by the
+ * parity tests); BK_TMA_ROW=0 selects per-brick staging for FP32 / BF16, BK_TMA_STAGES
+ * (2..4) and BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernels. */
 int bk_sweep(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
              const unsigned *blist, unsigned nlist, const bk_stencil *st, const bk_layout *lay,
              int acc, void *stream);
 
 /* Which kernel bk_sweep would launch for these fields, stencil, layout and accumulation
- * (no launch): *name = "sweep_star_tma_kernel", "sweep2_kernel" or "sweep_kernel" (a
- * static string).  No reference counterpart: a diagnostic of this implementation. */
+ * (no launch): *name = "sweep_star_row_kernel", "sweep_star_tma_kernel", "sweep2_kernel" or
+ * "sweep_kernel" (a static string).  No reference counterpart: a diagnostic of this implementation. */
 int bk_sweep_kernel(const bk_field *in, const bk_field *out, const bk_stencil *st, const bk_layout *lay,
                     int acc, const char **name);
 
