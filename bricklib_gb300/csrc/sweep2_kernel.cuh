@@ -43,6 +43,19 @@ __device__ __forceinline__ float to_acc(__nv_bfloat16 x) { return __bfloat162flo
 __device__ __forceinline__ float to_acc(float x) { return x; }
 __device__ __forceinline__ double to_acc(double x) { return x; }
 
+// Two adjacent elements (i, i+1) of a brick row in FP32: one 8-byte (FP32) or 4-byte (BF16)
+// shared-memory load, one store of the same width.  bf16 -> fp32 is exact (the bf16 bits are
+// the high half of the fp32 word); fp32 -> bf16 rounds to nearest even as the scalar path.
+__device__ __forceinline__ float2 ld_pair(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ float2 ld_pair(const __nv_bfloat16 *p) {
+  const unsigned u = *reinterpret_cast<const unsigned *>(p);
+  return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xFFFF0000u));
+}
+__device__ __forceinline__ void st_pair(float *p, float2 v) { __stcs(reinterpret_cast<float2 *>(p), v); }
+__device__ __forceinline__ void st_pair(__nv_bfloat16 *p, float2 v) {
+  *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(v.x, v.y);
+}
+
 __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
@@ -68,6 +81,13 @@ __host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, in
   return need;
 }
 
+// bricks (warps) per CTA of the column-pair cube kernels: one, so that a CTA's barriers wait
+// for no other warp (GB300, FP32 cube125 at 512^3: 191 / 171 GStencil/s with one / two)
+#ifndef BK_PAIR_NB
+#define BK_PAIR_NB 1
+#endif
+constexpr int PAIR_NB = BK_PAIR_NB;
+
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
 struct Sweep2Cfg {
   static constexpr int ES = (int)sizeof(T);
@@ -86,7 +106,14 @@ struct Sweep2Cfg {
                                  : conflict_free_row(NEED, BI, ES, VE);
   static constexpr int TILE = EK * EJ * EI;  // elements per brick tile
   static constexpr int TILE_BYTES = (TILE * ES + 15) / 16 * 16;
-  static constexpr int TPB = BJ * BI;
+  // Column pairs: one warp per 8x8x8 brick, each lane computing columns (i0, i0 + 1) from
+  // 8-byte (FP32) / 4-byte (BF16) row loads, for the cubes whose per-plane row values or
+  // symmetry-class sums fit a sliding window along k (FP32 arithmetic on 2- and 4-byte
+  // storage; GB300 at 512^3, GStencil/s against one column per thread: FP32 cube27 313 / 287,
+  // cube125 191 / 156; BF16 cube27 412 / 302, cube125 235 / 139).
+  static constexpr bool PAIR = ES <= 4 && BK == 8 && BJ == 8 && BI == 8 && ACC == ACCM_NATIVE &&
+                               (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ || (FAM == FAM_CUBE && R == 1));
+  static constexpr int TPB = PAIR ? BJ * BI / 2 : BJ * BI;
   // vectors of the neighbourhood (per brick)
   static constexpr int NV_CENTRE = BK * BJ * (BI / VE);
   static constexpr int NV_KF = R * BJ * (BI / VE);   // one k face
@@ -100,7 +127,7 @@ struct Sweep2Cfg {
   static constexpr int FTILE_BYTES = 0;
   // bricks per CTA: as many as fit 128 threads and a ~100 KB shared-memory budget
   static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 36 * 4;
-  static constexpr int NB = cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
+  static constexpr int NB = PAIR ? PAIR_NB : cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
   static constexpr int NT = TPB * NB;
   static constexpr int SMEM = NB * PER_BRICK;
 };
@@ -179,14 +206,131 @@ __device__ __forceinline__ unsigned plan_entry(int g) {
   return slot | (src << 5) | (dst << 18);
 }
 
-// One brick's outputs from its staged tile (the compute of sweep2_kernel, shared with the
-// warp-specialised kernel): each of the BJ*BI threads (lt) owns one (j, i) column.
+// Columns (i0, i0 + 1) of row j of one 8x8x8 brick, every k, from its staged tile, in FP32
+// arithmetic: mirror-symmetric cubes (radius 1 or 2, pair sums) and the radius-1 cube.  Plane
+// kk of the tile yields the 2R + 2 values x(kk, j + dj, i0 - R .. i0 + 1 + R) of every row
+// dj = -R..R (aligned pair loads); a symmetric cube reduces them at once to its class sums
+// q(kk).  Output plane k is complete once plane k + 2R is in, and is then summed term by term
+// in the order of the one-column code below (class by class: c0 q(k), then c_d (q(k-d) +
+// q(k+d)); the plain cube: dj, di, dk), so both give identical results.  Only the last 2R + 1
+// planes are live.
+template <typename C, typename T, int R, int FAM>
+__device__ __forceinline__ void cube_pair_columns(const T *rt, T *ob, const int j, const int i0, const Taps &tp) {
+  constexpr int BK = 8, PK = 64, SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP;
+  constexpr int NK = BK + 2 * R, NR = 2 * R + 1, W = 2 * R + 2;
+  static_assert(R == 1 || R == 2, "cube radius");
+  const T *col = rt + (j + R) * SJ + (i0 + RP);  // (plane 0, row j, column i0)
+  // x[kk][r][m] = x(kk, j + r - R, i0 + m - R)
+  float x[NK][NR][W];
+  auto load_plane = [&](int kk) {
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const T *p = col + kk * SK + (r - R) * SJ;
+      if constexpr (R == 1) {
+        const float2 c = ld_pair(p);
+        x[kk][r][0] = to_acc(p[-1]);
+        x[kk][r][1] = c.x;
+        x[kk][r][2] = c.y;
+        x[kk][r][3] = to_acc(p[2]);
+      } else {
+        const float2 l = ld_pair(p - 2), c = ld_pair(p), h = ld_pair(p + 2);
+        x[kk][r][0] = l.x;
+        x[kk][r][1] = l.y;
+        x[kk][r][2] = c.x;
+        x[kk][r][3] = c.y;
+        x[kk][r][4] = h.x;
+        x[kk][r][5] = h.y;
+      }
+    }
+  };
+  if constexpr (FAM == FAM_CUBE) {
+#pragma unroll
+    for (int kk = 0; kk < NK; ++kk) {
+      load_plane(kk);
+      if (kk >= 2 * R) {
+        const int k = kk - 2 * R;
+        float acc[2];
+#pragma unroll
+        for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+          for (int di = -R; di <= R; ++di)
+#pragma unroll
+            for (int dk = -R; dk <= R; ++dk) {
+              const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+              const float c = coef<float>(tp, t);
+#pragma unroll
+              for (int o = 0; o < 2; ++o) {
+                const float v = x[k + R + dk][dj + R][R + o + di];
+                acc[o] = (dj == -R && di == -R && dk == -R) ? c * v : fmaf(c, v, acc[o]);
+              }
+            }
+        st_pair(ob + k * PK, make_float2(acc[0], acc[1]));
+      }
+    }
+  } else {
+    constexpr bool IJ = FAM == FAM_CUBESYM_IJ;
+    constexpr int NC = IJ ? (R + 1) * (R + 2) / 2 : (R + 1) * (R + 1);
+    float q[NC][NK][2];
+    // sum of x(kk, j +- b, i +- a) over the distinct sign choices, for output column i0 + o
+    auto ring = [&](int kk, int b, int a, int o) -> float {
+      const int m = R + o;
+      if (a == 0 && b == 0) return x[kk][R][m];
+      if (b == 0) return x[kk][R][m - a] + x[kk][R][m + a];
+      if (a == 0) return x[kk][R - b][m] + x[kk][R + b][m];
+      return (x[kk][R - b][m - a] + x[kk][R - b][m + a]) + (x[kk][R + b][m - a] + x[kk][R + b][m + a]);
+    };
+#pragma unroll
+    for (int kk = 0; kk < NK; ++kk) {
+      load_plane(kk);
+      {
+        int cls = 0;
+#pragma unroll
+        for (int b = 0; b <= R; ++b)
+#pragma unroll
+          for (int a = 0; a <= (IJ ? b : R); ++a, ++cls)
+#pragma unroll
+            for (int o = 0; o < 2; ++o)
+              q[cls][kk][o] = (IJ && a != b) ? ring(kk, b, a, o) + ring(kk, a, b, o) : ring(kk, b, a, o);
+      }
+      if (kk >= 2 * R) {
+        const int k = kk - 2 * R;
+        float acc[2];
+        int cls = 0;
+#pragma unroll
+        for (int b = 0; b <= R; ++b)
+#pragma unroll
+          for (int a = 0; a <= (IJ ? b : R); ++a, ++cls) {
+            const float c0 = coef<float>(tp, sym_index(0, b, a, R));
+#pragma unroll
+            for (int o = 0; o < 2; ++o)
+              acc[o] = (a == 0 && b == 0) ? c0 * q[cls][k + R][o] : fmaf(c0, q[cls][k + R][o], acc[o]);
+#pragma unroll
+            for (int d = 1; d <= R; ++d) {
+              const float cd = coef<float>(tp, sym_index(d, b, a, R));
+#pragma unroll
+              for (int o = 0; o < 2; ++o) acc[o] = fmaf(cd, q[cls][k + R - d][o] + q[cls][k + R + d][o], acc[o]);
+            }
+          }
+        st_pair(ob + k * PK, make_float2(acc[0], acc[1]));
+      }
+    }
+  }
+}
+
+// One brick's outputs from its staged tile (the compute of sweep2_kernel): each of the BJ*BI
+// threads (lt) owns one (j, i) column, or, for the column-pair cubes, each of the BJ*BI/2
+// threads a pair of columns.
 // out_brick: the output field's brick (field base + centre brick x step).
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
 __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, const Taps &tp) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
   typedef typename Elem<T>::acc AT;
   constexpr int EJ = C::EJ, EI = C::EI, SK = EJ * EI, SJ = EI, RP = C::RP;
+  if constexpr (C::PAIR) {
+    const int jp = lt >> 2, i0 = 2 * (lt & 3);
+    cube_pair_columns<C, T, R, FAM>(rt, out_brick + (size_t)(jp * BI + i0), jp, i0, tp);
+    return;
+  }
   int j = lt / BI;
   const int i = lt - j * BI;
   if (C::PERM) j = (j & ~3) | ((j & 1) << 1) | ((j >> 1) & 1);  // rows 0,2,1,3 per warp

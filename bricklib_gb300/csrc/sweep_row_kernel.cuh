@@ -44,19 +44,6 @@ struct RowTmaCfg {
   static constexpr int smem(int stages) { return 128 + stages * STAGE + META; }
 };
 
-// Two adjacent elements (i, i+1) of a brick row in FP32: one 8-byte (FP32) or 4-byte (BF16)
-// shared-memory load, one store of the same width.  bf16 -> fp32 is exact (the bf16 bits are
-// the high half of the fp32 word); fp32 -> bf16 rounds to nearest even as the scalar path.
-__device__ __forceinline__ float2 ld_pair(const float *p) { return *reinterpret_cast<const float2 *>(p); }
-__device__ __forceinline__ float2 ld_pair(const __nv_bfloat16 *p) {
-  const unsigned u = *reinterpret_cast<const unsigned *>(p);
-  return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xFFFF0000u));
-}
-__device__ __forceinline__ void st_pair(float *p, float2 v) { __stcs(reinterpret_cast<float2 *>(p), v); }
-__device__ __forceinline__ void st_pair(__nv_bfloat16 *p, float2 v) {
-  *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(v.x, v.y);
-}
-
 // Element offsets (from the stage base, plane 0) of one thread's taps for columns (i0, i0+1):
 // a[m + MI] = the aligned pair (i0 + 2m, i0 + 2m + 1), m = -MI..MI, MI = ceil(R/2) (m = 0 is the
 // centre; the others may sit in the slots either side); oj / sj the j taps (index 2(d-1) is +d,
