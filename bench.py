@@ -235,7 +235,7 @@ def run_ours(args):
     dom_ms = per_shape_ms[dom]
     achieved = points * bytes_pt / (dom_ms * 1e-3) / 1e9
     tr = traffic_table().get(f"{args.dtype}:{args.acc}:{dom}:{n}")
-    instr = fp_instructions_per_point(sts[dom], acc)
+    instr = fp_instructions_per_point(sts[dom], acc, dtype)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": tr,
                 "kernel": f"{B.sweepKernel(b_in, b_out, csts[dom], acc)} {dom}",
@@ -285,8 +285,9 @@ def run_ours(args):
 
     # end to end through the public API, every result in host memory.  Per step: the input is
     # copied from page-locked memory (on a copy stream, into one of two device buffers, while the
-    # previous step sweeps); each sweep but the last writes a device buffer (two, ping-pong) whose
-    # device-to-host copy runs on a second copy stream under the next sweep; the last sweep
+    # previous step sweeps); each sweep but the last writes its own device buffer, whose
+    # device-to-host copy runs on a second copy stream under the following sweeps (one buffer per
+    # stencil, so no sweep waits for an earlier result to leave its buffer); the last sweep
     # stores its result straight into mapped page-locked host memory (bk_host_malloc) over
     # NVLink-C2C.  The link carries the input and the results in opposite directions.
     e2e = None
@@ -296,7 +297,9 @@ def run_ours(args):
         s_in2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
         ins = [B.Brick(dinfo, s_in, 0, lay), B.Brick(dinfo, s_in2, 0, lay)]
         s_out2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
-        outs = [B.Brick(dinfo, s_out, 0, lay), B.Brick(dinfo, s_out2, 0, lay)]
+        nbuf = max(2, len(shapes) - 1)
+        s_outs = [s_out, s_out2] + [B.BrickStorage.allocate_device(nbricks, bsize, dtype) for _ in range(nbuf - 2)]
+        outs = [B.Brick(dinfo, so, 0, lay) for so in s_outs]
         h_outs = {}
         for name in shapes:
             h_outs[name] = B.BrickStorage.allocate_pinned(nbricks, bsize, dtype)
@@ -306,8 +309,8 @@ def run_ours(args):
         cin, cout = torch.cuda.Stream(), torch.cuda.Stream()
         arrived = [torch.cuda.Event(), torch.cuda.Event()]
         consumed = [torch.cuda.Event(), torch.cuda.Event()]
-        swept = [torch.cuda.Event(), torch.cuda.Event()]
-        copied = [torch.cuda.Event(), torch.cuda.Event()]
+        swept = [torch.cuda.Event() for _ in range(nbuf)]
+        copied = [torch.cuda.Event() for _ in range(nbuf)]
         Ke = max(1, min(K, 5))
 
         def h2d(buf):
@@ -317,6 +320,7 @@ def run_ours(args):
 
         for q in range(2):
             consumed[q].record(stream)
+        for q in range(nbuf):
             copied[q].record(stream)
         h2d(0)
         for it in range(Ke + 1):
@@ -332,7 +336,7 @@ def run_ours(args):
                 if q == len(shapes) - 1:
                     B.brickSweep(ins[cur], B.Brick(dinfo, h_outs[name], 0, lay), blist, csts[name], acc, stream=sp)
                     continue
-                ob = q % 2
+                ob = q % nbuf
                 stream.wait_event(copied[ob])  # its previous result has left the buffer
                 B.brickSweep(ins[cur], outs[ob], blist, csts[name], acc, stream=sp)
                 swept[ob].record(stream)
@@ -340,7 +344,7 @@ def run_ours(args):
                 B.memcpy(h_outs[name].ptr, outs[ob].bStorage.ptr, nbytes, 1, cout.cuda_stream)
                 copied[ob].record(cout)
             consumed[cur].record(stream)
-        for q in range(2):
+        for q in range(nbuf):
             stream.wait_event(copied[q])
         e1.record(stream)
         torch.cuda.synchronize()
@@ -368,8 +372,9 @@ def run_ours(args):
                "link_alone": link,
                "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a copy "
                        "stream under the previous step's sweeps; results: device-to-host copies on a second "
-                       "stream under the next sweep, the last sweep storing straight into mapped page-locked "
-                       "host memory over NVLink-C2C; one host buffer per stencil"}
+                       "stream under the following sweeps (one device buffer per stencil), the last sweep "
+                       "storing straight into mapped page-locked host memory over NVLink-C2C; one host buffer "
+                       "per stencil"}
 
     # CPU baseline: the oracle's OpenMP brick sweep on a sample of the same bricks,
     # also used as a spot check of the GPU output on those bricks
@@ -396,10 +401,11 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def fp_instructions_per_point(st, acc) -> float:
+def fp_instructions_per_point(st, acc, dtype=None) -> float:
     """Floating-point instructions per point of the kernel that runs `st` (native arithmetic on
     8x8x8 row-major bricks): a multiply-add per tap, except mirror-symmetric cubes, which the
-    pipelined kernel evaluates from pair sums (sweep2_kernel.cuh, FAM_CUBESYM)."""
+    pipelined kernel evaluates from pair sums (sweep2_kernel.cuh, FAM_CUBESYM); for FP64
+    storage it also shares the row sums of a column pair (sym_cube_pair_shared)."""
     from bricklib_gb300 import _abi
     taps = [tuple(t) for t in st.taps]
     r = st.radius
@@ -410,6 +416,8 @@ def fp_instructions_per_point(st, acc) -> float:
     if any(c[t] != c[tuple(abs(a) for a in t)] for t in taps):
         return float(len(taps))
     ij = all(c[(k, j, i)] == c[(k, i, j)] for (k, j, i) in taps)
+    if dtype == _abi.BK_F64:
+        return {(1, False): 17.0, (1, True): 15.25, (2, False): 63.0, (2, True): 52.5}[(r, ij)]
     return {(1, False): 18.25, (1, True): 16.5, (2, False): 69.0, (2, True): 58.5}[(r, ij)]
 
 
