@@ -32,10 +32,11 @@
 
 namespace bk {
 
-// The box shapes over one input field: whole brick, k face, j face (3-D view) and the
-// narrow i face (4-D view).
+// The box shapes over one input field: whole brick, k face, j face (3-D view), the narrow
+// i face (4-D view), and for the row-run kernel the same three 3-D boxes spanning a run of
+// consecutive bricks (NB + 2 whole bricks, NB k faces, NB j faces).
 struct TmaMaps {
-  CUtensorMap m[4];
+  CUtensorMap m[7];
 };
 
 constexpr int TMA_MAX_STAGES = 4;
@@ -457,6 +458,11 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
 // Host: encode the four box shapes over the input field.  Returns false when the field
 // does not meet the bulk-tensor rules (16-byte aligned base, strides multiple of 16 bytes).
 bool star_tma_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r, int iw, TmaMaps *maps);
+// The run boxes m[4..6] over consecutive bricks (after star_tma_maps): slot_box whole bricks, nb
+// k faces, nb j faces; false when the field cannot be described that way (the kernel then
+// copies brick by brick).
+bool row_group_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r, int nb, int slot_box,
+                    TmaMaps *maps);
 // Pipeline depth: BK_TMA_STAGES (2..4) when set, else `dflt`.
 int tma_stages(int dflt);
 

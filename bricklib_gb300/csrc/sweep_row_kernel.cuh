@@ -8,10 +8,14 @@
 // (slot 12).  One pipeline stage holds one run of L bricks:
 //   slots 0 .. L+1  whole bricks: the run's i-lo neighbour, the L centre bricks, the run's
 //                   i-hi neighbour (box (BJ*BI, BK) of the 3-D view (j*BI + i, k, brick));
-//   face block n    brick n's k faces (box (BJ*BI, R)) and j faces (box (R*BI, BK)).
+//   faces           brick n's k faces (box (BJ*BI, R)) and j faces (box (R*BI, BK)), each
+//                   type in its own array of NB.
 // Brick n's i taps read the slots either side of its own, so a run loads L + 2 whole bricks
 // where per-brick staging loads 3 L.  A list that is not in grid order runs as runs of one
-// brick.  Persistent CTAs, warp-specialised like the per-brick kernel: the last warp produces
+// brick.  A run of NB bricks whose slots are consecutive bricks in storage, and whose k / j
+// neighbours are too (a dense grid in grid order), takes five copies instead of 5 NB + 2: the
+// NB + 2 slots, and each face type of the NB bricks, as one box over consecutive bricks; the
+// copy-instruction rate, not the bytes, bounds this staging.  Persistent CTAs, warp-specialised like the per-brick kernel: the last warp produces
 // (lanes 0 .. 7*NB-1 each own one (entry, region) pair of the segment; list and adjacency
 // entries load several segments ahead), the other warps consume (brick slot n+1 belongs to
 // consumer warp n, whose lanes compute one (j, i, i+1) column pair each).  The number of
@@ -24,6 +28,12 @@
 
 namespace bk {
 
+// bricks per copy of a run's whole-brick slots (divides NB + 2)
+#ifndef BK_ROW_SLOT_BOX
+#define BK_ROW_SLOT_BOX 6
+#endif
+constexpr int SLOT_BOX = BK_ROW_SLOT_BOX;
+
 template <typename T, int R>
 struct RowTmaCfg {
   static constexpr int BK = 8, BJ = 8, BI = 8, PK = BJ * BI;
@@ -33,11 +43,12 @@ struct RowTmaCfg {
   static constexpr int NT = NC + 32;     // + the producer warp
   static constexpr int al(int b) { return (b + 127) / 128 * 128; }
   static constexpr int B_C = BK * BJ * BI * ES, B_KF = R * BJ * BI * ES, B_JF = BK * R * BI * ES;
-  static constexpr int PC = al(B_C);     // pitch of the whole-brick slots
-  static constexpr int O_KL = 0, O_KH = al(B_KF), O_JL = 2 * al(B_KF), O_JH = O_JL + al(B_JF);
-  static constexpr int PF = O_JH + al(B_JF);         // pitch of the face blocks
-  static constexpr int FACES = (NB + 2) * PC;        // face blocks after the slots
-  static constexpr int STAGE = FACES + NB * PF;      // bytes of one stage
+  static constexpr int PC = B_C;         // pitch of the whole-brick slots
+  // faces after the slots, by type: NB k-lo faces, NB k-hi, NB j-lo, NB j-hi (a run of
+  // consecutive bricks fills each type with one copy)
+  static constexpr int FKL = (NB + 2) * PC, FKH = FKL + NB * B_KF, FJL = FKH + NB * B_KF, FJH = FJL + NB * B_JF;
+  static constexpr int STAGE = FJH + NB * B_JF;      // bytes of one stage
+  static_assert(B_C % 128 == 0 && B_KF % 128 == 0 && B_JF % 128 == 0, "copies land on 128-byte boundaries");
   static constexpr int TXB = B_C + 2 * (B_KF + B_JF);  // bytes one run brick brings
   // after the stages: full[4], empty[4] mbarriers, centre brick index [4][NB], abort word
   static constexpr int META = 64 + 4 * TMA_MAX_STAGES * NB + 16;
@@ -131,7 +142,8 @@ __device__ __forceinline__ void star_pair_column(const T *f, const RowPairTaps<R
 
 template <typename T, int R, int ACC>
 __global__ void __launch_bounds__(RowTmaCfg<T, R>::NT)
-sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp, const int S) {
+sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp, const int S,
+                      const int group_maps) {
   typedef RowTmaCfg<T, R> C;
   constexpr int NB = C::NB, BK = C::BK, BJ = C::BJ, BI = C::BI, PK = C::PK, E = C::ES;
   constexpr unsigned NONE = 0xFFFFFFFFu;  // slot without a brick in this stage
@@ -172,7 +184,9 @@ sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     const int pslot = prg == 0 ? 13 : prg == 1 ? 4 : prg == 2 ? 22 : prg == 3 ? 10 : prg == 4 ? 16 : prg == 5 ? 12 : 14;
     const int pmap = prg == 1 || prg == 2 ? 1 : prg == 3 || prg == 4 ? 2 : 0;
     const int px = prg == 3 ? (BJ - R) * BI : 0, py = prg == 1 ? BK - R : 0;
-    const int poff = prg == 1 ? C::O_KL : prg == 2 ? C::O_KH : prg == 3 ? C::O_JL : C::O_JH;  // faces only
+    // faces only: the type's array and its pitch
+    const int fbase = prg == 1 ? C::FKL : prg == 2 ? C::FKH : prg == 3 ? C::FJL : C::FJH;
+    const int fpitch = prg == 1 || prg == 2 ? C::B_KF : C::B_JF;
     auto load_b = [&](long long grp) -> unsigned {
       const long long n = grp * NB + pbs;
       return (prod && grp < nseg && n < (long long)a.nlist) ? a.blist[n] : NONE;
@@ -250,8 +264,25 @@ sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
         const unsigned bar = full0 + 8 * st;
         if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)(L * C::TXB + 2 * C::B_C));
         __syncwarp();
-        if (prod && pbs >= s0 && pbs < e) {
-          const unsigned stage = sbase + st * C::STAGE;
+        // a full run over consecutive bricks: entry n's region r is region r of entry 0 plus
+        // n, and the slots run from the i-lo neighbour to the i-hi one without a gap
+        bool group = false;
+        if (group_maps && L == NB) {
+          const unsigned first = __shfl_sync(ALL, v, prg < 7 ? prg : 0);  // region prg of entry 0
+          const unsigned c0 = __shfl_sync(ALL, v, 0), cl = __shfl_sync(ALL, v, 7 * (NB - 1));
+          const bool ok = !prod || (prg <= 4 ? v == first + (unsigned)pbs
+                                             : prg == 5 ? (pbs != 0 || v + 1u == c0) : (pbs != NB - 1 || v == cl + 1u));
+          group = __all_sync(ALL, ok);
+        }
+        const unsigned stage = sbase + st * C::STAGE;
+        if (group) {
+          if (lane == 5)  // slots 0 .. NB+1, SLOT_BOX bricks per copy
+#pragma unroll
+            for (int q = 0; q < (NB + 2) / SLOT_BOX; ++q)
+              tma_load_3d(stage + q * SLOT_BOX * C::PC, &maps.m[4], 0, 0, (int)v + q * SLOT_BOX, bar);
+          else if (lane >= 1 && lane <= 4)
+            tma_load_3d(stage + fbase, &maps.m[pmap + 4], px, py, (int)v, bar);
+        } else if (prod && pbs >= s0 && pbs < e) {
           const int slot = pbs - s0 + 1;
           if (prg == 0) tma_load_3d(stage + slot * C::PC, &maps.m[0], 0, 0, (int)v, bar);
           else if (prg == 5) {
@@ -259,7 +290,7 @@ sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
           } else if (prg == 6) {
             if (pbs == e - 1) tma_load_3d(stage + (L + 1) * C::PC, &maps.m[0], 0, 0, (int)v, bar);
           } else {
-            tma_load_3d(stage + C::FACES + (slot - 1) * C::PF + poff, &maps.m[pmap], px, py, (int)v, bar);
+            tma_load_3d(stage + fbase + (slot - 1) * fpitch, &maps.m[pmap], px, py, (int)v, bar);
           }
         }
         ++it;
@@ -299,7 +330,7 @@ sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
   const int slot = bs + 1;
   constexpr int SE = C::PC / E;  // slot pitch in elements
   constexpr int MI = (R + 1) / 2;
-  const int fb = (C::FACES + bs * C::PF) / E;
+
   RowPairTaps<R> o;
 #pragma unroll
   for (int m = -MI; m <= MI; ++m) {
@@ -312,13 +343,13 @@ sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     for (int sg = 0; sg < 2; ++sg) {
       const int q = 2 * (d - 1) + sg;
       const int jj = sg ? j - d : j + d;
-      if (jj >= BJ) { o.oj[q] = fb + C::O_JH / E + (jj - BJ) * BI + i0; o.sj[q] = R * BI; }
-      else if (jj < 0) { o.oj[q] = fb + C::O_JL / E + (R + jj) * BI + i0; o.sj[q] = R * BI; }
+      if (jj >= BJ) { o.oj[q] = (C::FJH + bs * C::B_JF) / E + (jj - BJ) * BI + i0; o.sj[q] = R * BI; }
+      else if (jj < 0) { o.oj[q] = (C::FJL + bs * C::B_JF) / E + (R + jj) * BI + i0; o.sj[q] = R * BI; }
       else { o.oj[q] = slot * SE + jj * BI + i0; o.sj[q] = PK; }
     }
   }
-  o.kl = fb + C::O_KL / E + j * BI + i0;
-  o.kh = fb + C::O_KH / E + j * BI + i0;
+  o.kl = (C::FKL + bs * C::B_KF) / E + j * BI + i0;
+  o.kh = (C::FKH + bs * C::B_KF) / E + j * BI + i0;
 
   int st = 0;
   unsigned ph = 0;
@@ -347,12 +378,21 @@ sweep_star_row_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
 template <typename T, int R, int ACC>
 int launch_star_row(const SweepArgs &a, const Taps &tp, int dtype, cudaStream_t s) {
   typedef RowTmaCfg<T, R> C;
-  const int S = tma_stages(2);
+  // Defaults measured on GB300 at 512^3 (GStencil/s, grouped copies with 2 / 3 stages, brick by
+  // brick with 2): FP32 star7 578 / 735 / 704, star13 635 / 629 / 619, star25 528 / 457 / 491;
+  // BF16 star7 938 / 921 / 821, star13 700 / 699 / 616, star25 483 / 481 / 503.
+  constexpr bool group_default = !(C::ES == 2 && R == 4);
+  const int S = tma_stages(C::ES == 4 && R == 1 ? 3 : 2);
   const int smem = C::smem(S);
   if (smem > 227 * 1024) return fail(BK_ERR_UNSUPPORTED, "row TMA sweep stages exceed shared memory");
   TmaMaps maps;
   if (!star_tma_maps(a, dtype, C::BK, C::BJ, C::BI, R, C::BI, &maps))
     return fail(BK_ERR_UNSUPPORTED, "field not describable to the TMA unit");
+  // BK_TMA_GROUP=0 / 1 keeps every run on brick-by-brick copies / allows grouped copies
+  const char *ge = getenv("BK_TMA_GROUP");
+  const bool group = ge ? ge[0] != '0' : group_default;
+  static_assert((C::NB + 2) % SLOT_BOX == 0, "slot copies");
+  const int group_maps = group && row_group_maps(a, dtype, C::BK, C::BJ, C::BI, R, C::NB, SLOT_BOX, &maps);
   auto kern = sweep_star_row_kernel<T, R, ACC>;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -365,7 +405,7 @@ int launch_star_row(const SweepArgs &a, const Taps &tp, int dtype, cudaStream_t 
   long long grid = (long long)sms * per_sm;
   if (grid > segs) grid = segs;
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, C::NT, smem, s>>>(maps, a, tp, S);
+  kern<<<(unsigned)grid, C::NT, smem, s>>>(maps, a, tp, S, group_maps);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "row TMA sweep launch");
   return BK_OK;

@@ -61,6 +61,32 @@ bool star_tma_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool row_group_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r, int nb, int slot_box,
+                    TmaMaps *maps) {
+  const EncodeTiledFn encode = encode_tiled();
+  if (!encode) return false;
+  const size_t es = dtype_size(dtype);
+  const CUtensorMapDataType ty = dtype == BK_F64   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                 : dtype == BK_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                                   : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  const char *base = reinterpret_cast<const char *>(a.in) + a.in_off * es;
+  const size_t plane = (size_t)bj * bi;
+  if (a.in_chunks < nb + 2) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)plane, (cuuint64_t)bk, (cuuint64_t)a.in_chunks};
+  const cuuint64_t strides[2] = {(cuuint64_t)(plane * es), (cuuint64_t)(a.in_step * es)};
+  const cuuint32_t boxes[3][3] = {{(cuuint32_t)plane, (cuuint32_t)bk, (cuuint32_t)slot_box},
+                                  {(cuuint32_t)plane, (cuuint32_t)r, (cuuint32_t)nb},
+                                  {(cuuint32_t)(r * bi), (cuuint32_t)bk, (cuuint32_t)nb}};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  for (int m = 0; m < 3; ++m) {
+    const CUresult e = encode(&maps->m[4 + m], ty, 3, const_cast<char *>(base), dims, strides, boxes[m], estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (e != CUDA_SUCCESS) return false;
+  }
+  return true;
+}
+
 int tma_stages(int dflt) {
   const char *e = getenv("BK_TMA_STAGES");
   if (!e) return dflt;

@@ -332,7 +332,8 @@ def _row_lists(dom, seed):
 def test_row_kernel_equals_per_brick_staging(dtype, acc, name, monkeypatch):
     """The row-run TMA kernel (runs of i-adjacent list entries share their whole-brick i
     faces) writes exactly what per-brick TMA staging and the pipelined kernel write, for
-    lists in grid order, shuffled, in grid-order pieces, with repeats and with a ragged tail."""
+    lists in grid order, shuffled, in grid-order pieces, with repeats and with a ragged tail;
+    full runs over consecutive bricks give the same with grouped and brick-by-brick copies."""
     st = stencils.make(name, 17)
     dom = GridDomain((64, 128, 128), dtype=dtype)  # 4,096 interior bricks
     arr = stencils.uniform(37, int(np.prod(dom.adims))).reshape(dom.adims)
@@ -349,6 +350,12 @@ def test_row_kernel_equals_per_brick_staging(dtype, acc, name, monkeypatch):
         piped = _sweep_with("BK_SWEEP_PIPELINED", monkeypatch, dom, st, acc, dl)
         np.testing.assert_array_equal(row.view(np.uint8), per_brick.view(np.uint8), err_msg=key)
         np.testing.assert_array_equal(row.view(np.uint8), piped.view(np.uint8), err_msg=key)
+        if key == "grid":  # full runs over consecutive bricks: grouped and brick-by-brick copies
+            for g in ("0", "1"):
+                monkeypatch.setenv("BK_TMA_GROUP", g)
+                other = _sweep_with(None, monkeypatch, dom, st, acc, dl)
+                monkeypatch.delenv("BK_TMA_GROUP")
+                np.testing.assert_array_equal(row.view(np.uint8), other.view(np.uint8), err_msg=f"group {g}")
         written = row.view(np.uint8).reshape(dom.nbricks, dom.nfields, -1)[:, 1, :]
         assert int(np.count_nonzero((written != 0xFF).any(axis=1))) == len(np.unique(lst)), key
 
