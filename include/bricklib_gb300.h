@@ -159,8 +159,9 @@ int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, in
  * their i-neighbour bricks; FP64: per-brick staging), a pipelined one (row-major layouts,
  * 16-byte aligned input) and a one-shot one (everything).  The environment variables
  * BK_SWEEP_ONESHOT=1 and BK_SWEEP_PIPELINED=1 override the built-in choice (used by the
- * parity tests); BK_TMA_ROW=0 selects per-brick staging for FP32 / BF16, BK_TMA_STAGES
- * (2..4) and BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernels. */
+ * parity tests); BK_TMA_ROW=0 selects per-brick staging for FP32 / BF16, BK_TMA_GROUP=0/1
+ * turns the row kernel's grouped copies of full runs off/on, BK_TMA_STAGES (2..4) and
+ * BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernels. */
 int bk_sweep(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
              const unsigned *blist, unsigned nlist, const bk_stencil *st, const bk_layout *lay,
              int acc, void *stream);
