@@ -590,7 +590,8 @@ def run_batched(args):
             "domains": len(w.domains), "interior_points": w.points, "steps": steps,
             "batched_fp32": {"value": round(gst_batch, 2), "ms_per_10_steps": round(t_batch * 1e3, 3),
                              "layout": {"bdim": lay.bdim, "fold": lay.fold, "grid_cap": best["grid_cap"]},
-                             "graph": True, "launches_per_step": 2},
+                             "graph": True, "periodic": "through the adjacency (no ghost fill)",
+                             "launches_per_step": len({d.stencil for d in w.domains})},
             "plain_fp64_per_domain": {"value": round(w.points * steps / t_plain64 / 1e9, 2),
                                       "ms": round(t_plain64 * 1e3, 2)},
             "unbatched_fp32_per_domain": {"value": round(w.points * steps / t_plain32 / 1e9, 2),

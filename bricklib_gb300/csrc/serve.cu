@@ -6,16 +6,18 @@
 //              adjacency and staging array come from the stream-ordered allocator on an
 //              admission stream, its input is copied in and scattered into bricks there,
 //              and the tick stream waits on that before the job's first step;
-//   ticks      every active job advances one step per tick: one batched ghost fill per
-//              storage type and one persistent sweep launch per (storage type, stencil)
-//              group over a work list of all active jobs' bricks.  Jobs join and leave
-//              between ticks, so work of jobs that arrived at different times overlaps;
+//   ticks      every active job advances one step per tick: one persistent sweep launch per
+//              (storage type, stencil) group over a work list of all active jobs' bricks.
+//              Jobs join and leave between ticks, so work of jobs that arrived at different
+//              times overlaps;
 //   retirement after its last step a job's newest field is gathered into an array and
 //              copied to the client's output on a retire stream; a host callback on that
 //              stream stamps the completion time, releases its budget and wakes waiters.
-// Domains use the init_grid layout (brick index = grid position) with one ghost brick
-// per side and periodic ghost fill.  No device-side wait exists: the only waits are host
-// waits with timeouts.
+// Domains use the init_grid layout (brick index = grid position, one ghost brick per side);
+// the periodic boundary goes through the adjacency, which points every interior brick's
+// neighbours across the boundary at the interior bricks a periodic ghost fill would copy,
+// so no fill runs between steps and the ghost bricks stay unused.  No device-side wait
+// exists: the only waits are host waits with timeouts.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -35,15 +37,22 @@ namespace bk {
 
 using Clock = std::chrono::steady_clock;
 
-// init_grid adjacency (bricksetup.h:44-47 rule) of a (gk, gj, gi) grid, brick = position.
+// Periodic adjacency of a (gk, gj, gi) brick grid (brick = position, one ghost brick per side):
+// the neighbour (k + dk, j + dj, i + di) of every brick, wrapped into the interior
+// 1 .. g - 2 of each axis.  For an interior brick this is the init_grid neighbour
+// (bricksetup.h:44-47) wherever that is interior, and the source of the periodic ghost fill
+// wherever it is a ghost brick.
 __global__ void grid_adj_kernel(unsigned *adj, int gk, int gj, int gi) {
   const long long size = (long long)gk * gj * gi;
+  const int nk = gk - 2, nj = gj - 2, ni = gi - 2;
   for (long long p = blockIdx.x * 256ll + threadIdx.x; p < size * 27; p += (long long)gridDim.x * 256) {
     const long long b = p / 27;
     const int s = (int)(p - b * 27);
     const int dk = s / 9 - 1, dj = (s / 3) % 3 - 1, di = s % 3 - 1;
-    const long long q = b + ((long long)dk * gj + dj) * gi + di;
-    adj[p] = (q >= 0 && q < size) ? (unsigned)q : 0u;
+    const int k = (int)(b / ((long long)gj * gi)), j = (int)((b / gi) % gj), i = (int)(b % gi);
+    const int wk = 1 + ((k + dk - 1) % nk + nk) % nk, wj = 1 + ((j + dj - 1) % nj + nj) % nj,
+              wi = 1 + ((i + di - 1) % ni + ni) % ni;
+    adj[p] = (unsigned)(((long long)wk * gj + wj) * gi + wi);
   }
 }
 
@@ -54,7 +63,7 @@ __global__ void identity_kernel(unsigned *g, long long n) {
 struct JobRow {
   unsigned dom;
   int gk, gj, gi;
-  unsigned long long work_off, fill_off;
+  unsigned long long work_off;
 };
 
 // interior bricks of every job, in position order
@@ -66,43 +75,6 @@ __global__ void expand_work_kernel(const JobRow *rows, unsigned nrows, uint2 *wo
     const int i = (int)(l % ni), j = (int)((l / ni) % nj), k = (int)(l / ((long long)ni * nj));
     const unsigned p = (unsigned)(((long long)(k + 1) * r.gj + (j + 1)) * r.gi + (i + 1));
     work[r.work_off + l] = make_uint2(r.dom, p);
-  }
-}
-
-// periodic ghost plan of every job: the shell of ghost positions, each with its wrapped source
-__global__ void expand_fill_kernel(const JobRow *rows, unsigned nrows, uint3 *fill) {
-  const JobRow r = rows[blockIdx.x];
-  const long long faces_k = 2ll * r.gj * r.gi, faces_j = 2ll * (r.gk - 2) * r.gi, faces_i = 2ll * (r.gk - 2) * (r.gj - 2);
-  const long long n = faces_k + faces_j + faces_i;
-  for (long long l = threadIdx.x; l < n; l += blockDim.x) {
-    int k, j, i;
-    long long m = l;
-    if (m < faces_k) {
-      const long long half = (long long)r.gj * r.gi;
-      k = m < half ? 0 : r.gk - 1;
-      m %= half;
-      j = (int)(m / r.gi);
-      i = (int)(m % r.gi);
-    } else if ((m -= faces_k) < faces_j) {
-      const long long half = (long long)(r.gk - 2) * r.gi;
-      j = m < half ? 0 : r.gj - 1;
-      m %= half;
-      k = 1 + (int)(m / r.gi);
-      i = (int)(m % r.gi);
-    } else {
-      m -= faces_j;
-      const long long half = (long long)(r.gk - 2) * (r.gj - 2);
-      i = m < half ? 0 : r.gi - 1;
-      m %= half;
-      k = 1 + (int)(m / (r.gj - 2));
-      j = 1 + (int)(m % (r.gj - 2));
-    }
-    const int sk = 1 + ((k - 1) % (r.gk - 2) + (r.gk - 2)) % (r.gk - 2);
-    const int sj = 1 + ((j - 1) % (r.gj - 2) + (r.gj - 2)) % (r.gj - 2);
-    const int si = 1 + ((i - 1) % (r.gi - 2) + (r.gi - 2)) % (r.gi - 2);
-    const unsigned dst = (unsigned)(((long long)k * r.gj + j) * r.gi + i);
-    const unsigned src = (unsigned)(((long long)sk * r.gj + sj) * r.gi + si);
-    fill[r.fill_off + l] = make_uint3(r.dom, dst, src);
   }
 }
 
@@ -164,10 +136,8 @@ struct bk_server {
   bool dirty = true;
   BatchDomain *d_doms = nullptr;
   uint2 *d_work = nullptr;
-  uint3 *d_fill = nullptr;
   JobRow *d_rows = nullptr;
   std::vector<std::pair<int, std::pair<unsigned, unsigned>>> work_seg;  // group -> (offset, count)
-  std::vector<std::pair<int, std::pair<unsigned, unsigned>>> fill_seg;  // dtype -> (offset, count)
   unsigned ndom = 0;
   int parity = 0;
   std::deque<cudaEvent_t> inflight;
@@ -191,9 +161,8 @@ static size_t job_bytes(const Layout &L, const Job &j) {
   const size_t es = dtype_size(j.dtype);
   const size_t bs = (size_t)L.size();
   const size_t interior = (size_t)(j.g[0] - 2) * (j.g[1] - 2) * (j.g[2] - 2);
-  const size_t ghost = (size_t)j.nbricks - interior;
   return (size_t)j.nbricks * (2 * bs * es + 27 * 4 + 4) + (size_t)j.n[0] * j.n[1] * j.n[2] * es +
-         interior * sizeof(uint2) + ghost * sizeof(uint3) + sizeof(BatchDomain) + 4096;
+         interior * sizeof(uint2) + sizeof(BatchDomain) + 4096;
 }
 
 static int group_of(bk_server *S, const Job &j) {
@@ -317,7 +286,7 @@ static unsigned char *ring_slot(bk_server *S, size_t bytes, int *slot) {
   return S->ring[r];
 }
 
-// rebuild the domain table, work list and fill list of the active jobs
+// rebuild the domain table and work list of the active jobs
 static int rebuild(bk_server *S) {
   cudaStream_t s = S->s_tick;
   std::vector<std::shared_ptr<Job>> order = S->active;
@@ -328,8 +297,7 @@ static int rebuild(bk_server *S) {
   std::vector<BatchDomain> doms(n);
   std::vector<JobRow> rows(n);
   S->work_seg.clear();
-  S->fill_seg.clear();
-  unsigned long long woff = 0, total_fill = 0;
+  unsigned long long woff = 0;
   for (unsigned d = 0; d < n; ++d) {
     const Job &j = *order[d];
     const size_t es = dtype_size(j.dtype);
@@ -338,40 +306,24 @@ static int rebuild(bk_server *S) {
     doms[d] = BatchDomain{j.adj, (unsigned)j.nbricks, (unsigned)j.group, j.flip ? Bf : A, j.flip ? A : Bf,
                           (unsigned long long)2 * S->L.size() * es, j.nbricks};
     const unsigned long long nint = (unsigned long long)(j.g[0] - 2) * (j.g[1] - 2) * (j.g[2] - 2);
-    rows[d] = JobRow{d, j.g[0], j.g[1], j.g[2], woff, 0};
+    rows[d] = JobRow{d, j.g[0], j.g[1], j.g[2], woff};
     if (S->work_seg.empty() || S->work_seg.back().first != j.group)
       S->work_seg.push_back({j.group, {(unsigned)woff, 0}});
     S->work_seg.back().second.second += (unsigned)nint;
     woff += nint;
   }
-  // fill list: grouped by storage type
-  unsigned long long foff = 0;
-  for (int dt : {BK_F64, BK_F32}) {
-    const unsigned long long start = foff;
-    for (unsigned d = 0; d < n; ++d) {
-      const Job &j = *order[d];
-      if (j.dtype != dt) continue;
-      rows[d].fill_off = foff;
-      foff += (unsigned long long)j.nbricks - (unsigned long long)(j.g[0] - 2) * (j.g[1] - 2) * (j.g[2] - 2);
-    }
-    if (foff > start) S->fill_seg.push_back({dt, {(unsigned)start, (unsigned)(foff - start)}});
-  }
-  total_fill = foff;
   // new device buffers (stream ordered); the previous ones are freed after the ticks using them
   if (S->d_doms) BK_CUDA(cudaFreeAsync(S->d_doms, s));
   if (S->d_work) BK_CUDA(cudaFreeAsync(S->d_work, s));
-  if (S->d_fill) BK_CUDA(cudaFreeAsync(S->d_fill, s));
   if (S->d_rows) BK_CUDA(cudaFreeAsync(S->d_rows, s));
   S->d_doms = nullptr;
   S->d_work = nullptr;
-  S->d_fill = nullptr;
   S->d_rows = nullptr;
   S->ndom = n;
   if (!n) return BK_OK;
   BK_CUDA(cudaMallocAsync((void **)&S->d_doms, sizeof(BatchDomain) * n, s));
   BK_CUDA(cudaMallocAsync((void **)&S->d_rows, sizeof(JobRow) * n, s));
   BK_CUDA(cudaMallocAsync((void **)&S->d_work, sizeof(uint2) * std::max<unsigned long long>(woff, 1), s));
-  BK_CUDA(cudaMallocAsync((void **)&S->d_fill, sizeof(uint3) * std::max<unsigned long long>(total_fill, 1), s));
   const size_t bytes = sizeof(BatchDomain) * n + sizeof(JobRow) * n;
   int slot = 0;
   unsigned char *h = ring_slot(S, bytes, &slot);
@@ -382,7 +334,6 @@ static int rebuild(bk_server *S) {
   BK_CUDA(cudaMemcpyAsync(S->d_rows, h + sizeof(BatchDomain) * n, sizeof(JobRow) * n, cudaMemcpyHostToDevice, s));
   BK_CUDA(cudaEventRecord(S->ring_ev[slot], s));
   expand_work_kernel<<<n, 256, 0, s>>>(S->d_rows, n, S->d_work);
-  expand_fill_kernel<<<n, 256, 0, s>>>(S->d_rows, n, S->d_fill);
   BK_CUDA(cudaGetLastError());
   S->active = order;
   return BK_OK;
@@ -390,11 +341,6 @@ static int rebuild(bk_server *S) {
 
 static int tick(bk_server *S) {
   cudaStream_t s = S->s_tick;
-  for (auto &fs : S->fill_seg) {
-    int st = batch_launch_fill(S->d_doms, S->ndom, S->d_fill + fs.second.first, fs.second.second, S->parity,
-                               (size_t)S->L.size() * dtype_size(fs.first), S->err, s);
-    if (st) return st;
-  }
   for (auto &ws : S->work_seg) {
     const Group &g = S->groups[ws.first];
     // job storages come from cudaMallocAsync and hold two whole-brick fields: aligned
@@ -654,7 +600,6 @@ int bk_server_destroy(bk_server *S) {
   for (auto ev : S->inflight) cudaEventDestroy(ev);
   if (S->d_doms) cudaFree(S->d_doms);
   if (S->d_work) cudaFree(S->d_work);
-  if (S->d_fill) cudaFree(S->d_fill);
   if (S->d_rows) cudaFree(S->d_rows);
   for (size_t r = 0; r < S->ring.size(); ++r) {
     if (S->ring[r]) cudaFreeHost(S->ring[r]);

@@ -148,6 +148,23 @@ def test_domain_alone_equals_domain_in_the_mix():
         b1.close()
 
 
+@pytest.mark.parametrize("lo,hi", [(16, 48), (8, 16)])
+def test_periodic_adjacency_equals_ghost_fill(lo, hi):
+    """The periodic boundary through the adjacency (no fill) and through ghost bricks refreshed
+    before every step give the same interior, bit for bit (8-cell edges: a domain one brick
+    wide, whose every neighbour is itself)."""
+    w = BT.make_workload(ndom=6, seed=21, lo=lo, hi=hi, multiple=8)
+    res = []
+    for wrap in (True, False):
+        b = BT.Batch(w, B.Layout(), BK_F32, wrap=wrap)
+        b.run(5)
+        B.synchronize()
+        res.append([f[ds.interior] for f, ds in zip(fields(b, b.parity), b.doms)])
+        b.close()
+    for x, y in zip(*res):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_batch_rejects_bad_domains():
     from bricklib_gb300 import _abi
     import ctypes as C
