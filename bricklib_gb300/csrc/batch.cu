@@ -1,7 +1,8 @@
 // Batched form: many independent domains of different sizes and stencils advanced
-// together.  One persistent sweep launch per step walks a global work list of
-// (domain, brick) pairs; one ghost-fill launch per step walks a global list of
-// (domain, dst, src) brick pairs; T steps are captured once into a CUDA graph and replayed.
+// together.  Persistent sweep launches walk a global work list of (domain, brick) pairs;
+// domains that keep ghost bricks add one ghost-fill launch per step over a global list of
+// (domain, dst, src) brick pairs (domains whose adjacency wraps the periodic boundary need
+// none); T steps are captured once into a CUDA graph and replayed.
 //
 // The work list is sorted by stencil; each step launches one persistent kernel per stencil
 // over that stencil's segment, specialised at compile time for its family and radius.  Each
