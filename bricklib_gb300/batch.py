@@ -78,7 +78,12 @@ class DomainStorage:
     every reference to a ghost brick points at the interior brick the fill would copy into it,
     so the sweep reads the same values and no fill runs (the ghost bricks stay unused)."""
 
-    def __init__(self, spec: DomainSpec, lay: B.Layout, dtype: int, wrap: bool = False):
+    @staticmethod
+    def bricks(spec: DomainSpec, lay: B.Layout) -> int:
+        return int(np.prod([spec.n[a] // lay.bdim[a] + 2 for a in range(3)]))
+
+    def __init__(self, spec: DomainSpec, lay: B.Layout, dtype: int, wrap: bool = False,
+                 storage: Optional[B.BrickStorage] = None):
         self.spec, self.lay, self.dtype = spec, lay, dtype
         nb = tuple(spec.n[a] // lay.bdim[a] for a in range(3))
         self.gdims = tuple(x + 2 for x in nb)
@@ -95,7 +100,8 @@ class DomainStorage:
         self.wrap = wrap
         self.pairs = pairs
         self.info = B.movBrickInfo(info)
-        self.storage = B.BrickStorage.allocate_device(self.nbricks, 2 * lay.size, dtype)
+        self.storage = storage if storage is not None else B.BrickStorage.allocate_device(self.nbricks, 2 * lay.size,
+                                                                                         dtype)
 
     def field(self, which: int) -> B.Brick:
         return B.Brick(self.info, self.storage, which * self.lay.size, self.lay)
@@ -118,9 +124,23 @@ class Batch:
     wrap=False asks for ghost bricks refreshed by a batched fill before every step."""
 
     def __init__(self, w: Workload, lay: B.Layout, dtype: int = BK_F32, acc: int = BK_ACC_NATIVE,
-                 grid_cap: int = 0, stream=None, init: bool = True, wrap: bool = True):
+                 grid_cap: int = 0, stream=None, init: bool = True, wrap: bool = True, arena: bool = True):
         self.w, self.lay, self.dtype = w, lay, dtype
-        self.doms = [DomainStorage(d, lay, dtype, wrap=wrap) for d in w.domains]
+        if arena:
+            # every domain a range of bricks of one storage: bk_batch then sweeps the batch as
+            # one brick set through the plain kernels (stars take the TMA-fed ones)
+            step = 2 * lay.size
+            counts = [DomainStorage.bricks(d, lay) for d in w.domains]
+            bb = step * B.ELEM_SIZE[B.dtype_of(dtype)]
+            self.arena = B.DeviceBuffer(sum(counts) * bb)
+            call("bk_memset", C.c_void_p(self.arena.ptr), 0, self.arena.nbytes, None)
+            firsts = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(int)
+            views = [B.BrickStorage(c, step, dtype, device=B.DeviceView(self.arena, f * bb, c * bb))
+                     for c, f in zip(counts, firsts)]
+            self.doms = [DomainStorage(d, lay, dtype, wrap=wrap, storage=v) for d, v in zip(w.domains, views)]
+        else:
+            self.arena = None
+            self.doms = [DomainStorage(d, lay, dtype, wrap=wrap) for d in w.domains]
         if init:
             for ds in self.doms:
                 init_domain(ds, stream)

@@ -232,6 +232,19 @@ def init_grid(dimlist: Sequence[int]) -> Tuple[np.ndarray, BrickInfo]:
     return grid, BrickInfo(size, adj)
 
 
+class DeviceView(DeviceBuffer):
+    """`nbytes` of another device buffer from byte `offset` on (not owned: the parent stays
+    alive as long as the view)."""
+
+    def __init__(self, parent: DeviceBuffer, offset: int, nbytes: int):
+        if offset < 0 or offset + nbytes > parent.nbytes:
+            raise ValueError("view outside its buffer")
+        self.parent, self.nbytes, self.ptr = parent, int(nbytes), parent.ptr + int(offset)
+
+    def free(self) -> None:
+        self.ptr = 0
+
+
 class BrickStorage:
     """`chunks` chunks of `step` elements (brick.h:53-82).  Host storage is a numpy
     array; device storage (movBrickStorage) a DeviceBuffer."""

@@ -9,6 +9,7 @@
 // CTA slot (BJ*BI threads, one brick at a time) resolves its own domain from the domain
 // table -- adjacency list, ping-pong fields, storage step -- so a CTA can hold bricks of
 // several domains.
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -236,6 +237,21 @@ struct bk_batch {
   bool aligned = true;  // every field base and step 16-byte aligned: the pipelined kernel applies
   int *err = nullptr;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, fill, parity) -> graph
+  // Arena mode: every domain's storage is a range of bricks of one storage (same step and
+  // field offsets).  The batch then is one brick set: a global adjacency (each domain's
+  // entries shifted by its first brick), global work and fill lists, and a step is the plain
+  // sweep (bk_sweep) per stencil segment and one plain ghost fill -- so star stencils take the
+  // TMA-fed kernels, which read whole bricks through one tensor map of the arena.
+  bool arena = false;
+  unsigned total = 0;             // bricks of the arena
+  unsigned *d_gadj = nullptr;     // total x 27
+  unsigned *d_gwork = nullptr;    // global brick ids, sorted by stencil (segments as seg)
+  unsigned *d_gpairs = nullptr;   // global (dst, src) pairs
+  unsigned ngpairs = 0;
+  bk_field field[2]{};            // field[0] at off0, field[1] at off1
+  std::vector<bk_stencil> csts;
+  int acc_mode = BK_ACC_NATIVE;
+  bk_layout lay{};
 };
 
 namespace bk {
@@ -272,6 +288,17 @@ int batch_launch_fill(const BatchDomain *doms, unsigned ndom, const uint3 *pairs
 }
 
 static int batch_sweep(bk_batch *b, cudaStream_t s) {
+  if (b->arena) {
+    const bk_field &fin = b->field[b->parity], &fout = b->field[b->parity ^ 1];
+    for (size_t q = 0; q < b->sts.size(); ++q) {
+      const unsigned first = b->seg[q].first, count = b->seg[q].second;
+      if (!count) continue;
+      const int st = bk_sweep(b->d_gadj, b->total, &fin, &fout, b->d_gwork + first, count, &b->csts[q], &b->lay,
+                              b->acc_mode, s);
+      if (st) return st;
+    }
+    return BK_OK;
+  }
   for (size_t q = 0; q < b->sts.size(); ++q) {
     const unsigned first = b->seg[q].first, count = b->seg[q].second;
     if (!count) continue;
@@ -284,6 +311,7 @@ static int batch_sweep(bk_batch *b, cudaStream_t s) {
 }
 
 static int batch_fill(bk_batch *b, cudaStream_t s) {
+  if (b->arena) return b->ngpairs ? bk_ghost_fill(b->d_gpairs, b->ngpairs, &b->field[b->parity], &b->lay, s) : BK_OK;
   if (!b->npairs) return BK_OK;
   const size_t bytes = (size_t)b->L.size() * dtype_size(b->dtype);
   const unsigned grid = b->npairs < (1u << 30) ? b->npairs : (1u << 30);
@@ -302,9 +330,100 @@ static void batch_free(bk_batch *b) {
   if (b->d_doms) cudaFree(b->d_doms);
   if (b->d_work) cudaFree(b->d_work);
   if (b->d_pairs) cudaFree(b->d_pairs);
+  if (b->d_gadj) cudaFree(b->d_gadj);
+  if (b->d_gwork) cudaFree(b->d_gwork);
+  if (b->d_gpairs) cudaFree(b->d_gpairs);
   b->d_doms = nullptr;
   b->d_work = nullptr;
   b->d_pairs = nullptr;
+  b->d_gadj = b->d_gwork = b->d_gpairs = nullptr;
+}
+
+// Adjacency of one arena domain: its entries shifted by the domain's first brick; an entry
+// outside the domain is clamped to the domain's brick 0 and flagged, as the sweeps do.
+__global__ void arena_adj_kernel(const unsigned *__restrict__ adj, unsigned nbricks, unsigned first,
+                                 unsigned *__restrict__ gadj, int *err) {
+  const size_t n = (size_t)nbricks * 27;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    unsigned v = adj[p];
+    if (v >= nbricks) {
+      atomicOr(err, FLAG_BOUNDS);
+      v = 0;
+    }
+    gadj[(size_t)first * 27 + p] = first + v;
+  }
+}
+
+// Arena mode when every domain's storage is a brick range of one storage (see bk_batch);
+// BK_OK also when the domains are not laid out that way (the batch then stays per domain).
+static int batch_arena(bk_batch *b, const bk_batch_domain *doms, unsigned ndom, const bk_stencil *sts, unsigned nst,
+                       const bk_layout *lay, int acc) {
+  const size_t es = dtype_size(b->dtype);
+  const bk_batch_domain &D0 = doms[0];
+  uintptr_t base = reinterpret_cast<uintptr_t>(D0.dat);
+  for (unsigned d = 1; d < ndom; ++d) base = std::min(base, reinterpret_cast<uintptr_t>(doms[d].dat));
+  const size_t stepb = D0.step * es;
+  std::vector<std::pair<unsigned long long, unsigned long long>> ranges(ndom);  // (first brick, end)
+  for (unsigned d = 0; d < ndom; ++d) {
+    const bk_batch_domain &D = doms[d];
+    const uintptr_t p = reinterpret_cast<uintptr_t>(D.dat);
+    if (D.step != D0.step || D.off0 != D0.off0 || D.off1 != D0.off1 || (p - base) % stepb || D.nbricks > (unsigned long long)D.chunks)
+      return BK_OK;
+    ranges[d] = {(p - base) / stepb, (p - base) / stepb + (unsigned long long)D.chunks};
+  }
+  std::vector<std::pair<unsigned long long, unsigned long long>> sorted = ranges;
+  std::sort(sorted.begin(), sorted.end());
+  for (unsigned d = 1; d < ndom; ++d)
+    if (sorted[d].first < sorted[d - 1].second) return BK_OK;  // overlapping domains
+  unsigned long long total = 0;
+  for (const auto &r : ranges) total = std::max(total, r.second);
+  if (total > 0x7FFFFFFFull) return BK_OK;
+  // host lists: global work per stencil, global fill pairs
+  std::vector<std::vector<unsigned>> per_st(nst);
+  std::vector<unsigned> gpairs;
+  for (unsigned d = 0; d < ndom; ++d) {
+    const bk_batch_domain &D = doms[d];
+    const unsigned first = (unsigned)ranges[d].first;
+    for (unsigned n = 0; n < D.nlist; ++n)
+      per_st[D.stencil].push_back(D.blist[n] < D.nbricks ? first + D.blist[n] : 0xFFFFFFFFu);
+    for (unsigned q = 0; q < D.npairs; ++q) {
+      const unsigned dst = D.pairs[2 * q], src = D.pairs[2 * q + 1];
+      gpairs.push_back(dst < D.nbricks ? first + dst : 0xFFFFFFFFu);
+      gpairs.push_back(src < D.nbricks ? first + src : 0xFFFFFFFFu);
+    }
+  }
+  std::vector<unsigned> gwork;
+  b->seg.clear();
+  for (unsigned q = 0; q < nst; ++q) {
+    b->seg.emplace_back((unsigned)gwork.size(), (unsigned)per_st[q].size());
+    gwork.insert(gwork.end(), per_st[q].begin(), per_st[q].end());
+  }
+  cudaError_t e = cudaMalloc(&b->d_gadj, sizeof(unsigned) * 27 * (size_t)total);
+  if (e == cudaSuccess) e = cudaMemset(b->d_gadj, 0, sizeof(unsigned) * 27 * (size_t)total);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_gwork, sizeof(unsigned) * (gwork.size() ? gwork.size() : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_gpairs, sizeof(unsigned) * (gpairs.size() ? gpairs.size() : 2));
+  if (e == cudaSuccess && gwork.size())
+    e = cudaMemcpy(b->d_gwork, gwork.data(), sizeof(unsigned) * gwork.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && gpairs.size())
+    e = cudaMemcpy(b->d_gpairs, gpairs.data(), sizeof(unsigned) * gpairs.size(), cudaMemcpyHostToDevice);
+  for (unsigned d = 0; d < ndom && e == cudaSuccess; ++d) {
+    const size_t n = (size_t)doms[d].nbricks * 27;
+    const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+    arena_adj_kernel<<<grid, 256>>>(doms[d].adj, doms[d].nbricks, (unsigned)ranges[d].first, b->d_gadj, b->err);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "bk_batch_create (arena)");
+  b->total = (unsigned)total;
+  b->ngpairs = (unsigned)(gpairs.size() / 2);
+  void *dat = reinterpret_cast<void *>(base);
+  b->field[0] = bk_field{dat, (long)total, D0.step, D0.off0, b->dtype};
+  b->field[1] = bk_field{dat, (long)total, D0.step, D0.off1, b->dtype};
+  b->csts.assign(sts, sts + nst);
+  b->acc_mode = acc;
+  b->lay = *lay;
+  b->arena = true;
+  return BK_OK;
 }
 
 }  // namespace bk
@@ -376,6 +495,11 @@ int bk_batch_create(bk_batch **out, const bk_batch_domain *doms, unsigned ndom, 
     batch_free(b);
     delete b;
     return fail(BK_ERR_CUDA, "device error word unavailable");
+  }
+  if ((s = batch_arena(b, doms, ndom, sts, nst, lay, acc)) != BK_OK) {
+    batch_free(b);
+    delete b;
+    return s;
   }
   *out = b;
   return BK_OK;

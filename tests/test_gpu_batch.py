@@ -165,6 +165,24 @@ def test_periodic_adjacency_equals_ghost_fill(lo, hi):
         np.testing.assert_array_equal(x, y)
 
 
+@pytest.mark.parametrize("wrap", [True, False])
+def test_arena_batch_equals_per_domain_storages(wrap):
+    """Domains as brick ranges of one arena (one brick set swept by the plain kernels, stars on
+    the TMA-fed ones) and domains in storages of their own (the batch-mode kernels) give the
+    same interiors bit for bit, with the boundary in the adjacency and with ghost fills."""
+    w = small_workload(nd=8)
+    res = []
+    for arena in (True, False):
+        b = BT.Batch(w, B.Layout(), BK_F32, wrap=wrap, arena=arena)
+        b.run(5)
+        B.synchronize()
+        assert B.error_flags() == 0
+        res.append([f[ds.interior] for f, ds in zip(fields(b, b.parity), b.doms)])
+        b.close()
+    for x, y in zip(*res):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_batch_rejects_bad_domains():
     from bricklib_gb300 import _abi
     import ctypes as C
