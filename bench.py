@@ -51,8 +51,9 @@ def parse():
     p.add_argument("--ndom", type=int, default=256)
     p.add_argument("--rates", default="200,2000")
     p.add_argument("--njobs", type=int, default=400)
-    p.add_argument("--form", default="plain", choices=["plain", "precision", "batched", "serving"],
-                   help="plain: the FP64 drop-in bench line; precision: the precision-form error study")
+    p.add_argument("--form", default="plain", choices=["plain", "precision", "batched", "serving", "next"],
+                   help="plain: the FP64 drop-in bench line; precision: the precision-form error study; "
+                        "next: array<->brick copies, ghost fill, BrickDecomp exchange and 4-D sweeps")
     return p.parse_args()
 
 
@@ -623,6 +624,106 @@ def run_serving(args):
                                   "50% FP64 / 50% FP32", "runs": res}), flush=True)
 
 
+def run_next(args):
+    """The rows beside the sweep, each timed on the device against the measured copy bandwidth:
+    device copyToBrick / copyFromBrick and a plain array copy (what stencils/copy.cpp times,
+    at 512^3 + 8 ghost + 8 padding, FP64), the periodic ghost fill of that domain, the periodic
+    exchange of a BrickDecomp of it, and the 4-D 9-point sweep (mpi9pt) on 64^4 bricks of 4^4."""
+    import torch
+    from bricklib_gb300 import _abi, bricks as B, bricks4 as B4, decomp as D
+    from bricklib_gb300._abi import call
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    call("bk_set_device", local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    hbm, peak_kind = peaks()
+    K = max(3, args.steps)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(K):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K * 1e-3
+
+    def rate(nbytes, sec):
+        return {"ms": round(sec * 1e3, 4), "gb_s": round(nbytes / sec / 1e9, 1), "hbm_frac": round(nbytes / sec / 1e9 / hbm, 4),
+                "bytes": int(nbytes)}
+
+    out = {"form": "next", "peak_hbm_gbs": hbm, "peak_source": f"{peak_kind} hbm_gbs", "steps": K, "warmup": args.warmup}
+    n, gz, pad = 512, 8, 8
+    g = n + 2 * gz
+    adim = g + 2 * pad
+    gb = g // 8
+    grid, info = B.init_grid([gb, gb, gb])
+    nb = info.nbricks
+    f64 = _abi.BK_F64
+    arr_in = B.DeviceBuffer(adim ** 3 * 8)
+    arr_out = B.DeviceBuffer(adim ** 3 * 8)
+    call("bk_fill_uniform", C.c_void_p(arr_in.ptr), adim ** 3, f64, 3, -1.0, 1.0, sp)
+    grid_dev = B.DeviceBuffer(grid.nbytes)
+    grid_dev.upload(np.ascontiguousarray(grid, dtype=np.uint32))
+    dinfo = B.movBrickInfo(info)
+    st = B.BrickStorage.allocate_device(nb, 512, f64)
+    brick = B.Brick(dinfo, st, 0)
+    moved = 2 * 8 * g ** 3  # every element of interior + ghost read once and written once
+    out["copy_to_bricks"] = rate(moved, timed(lambda: B.copyToBrickDevice([g] * 3, [pad] * 3, [0] * 3, arr_in.ptr,
+                                                                          grid_dev.ptr, brick, sp)))
+    out["copy_from_bricks"] = rate(moved, timed(lambda: B.copyFromBrickDevice([g] * 3, [pad] * 3, [0] * 3, arr_out.ptr,
+                                                                              grid_dev.ptr, brick, sp)))
+    out["array_copy"] = rate(2 * 8 * adim ** 3, timed(lambda: B.memcpy(arr_out.ptr, arr_in.ptr, adim ** 3 * 8, 2, sp)))
+    # the round trip is exact
+    back = np.empty(adim ** 3, np.float64)
+    ref = np.empty(adim ** 3, np.float64)
+    B.memcpy(back.ctypes.data, arr_out.ptr, back.nbytes, 1, sp)
+    B.memcpy(ref.ctypes.data, arr_in.ptr, ref.nbytes, 1, sp)
+    B.synchronize(sp)
+    sl = (slice(pad, pad + g),) * 3
+    out["copy_round_trip_exact"] = bool(np.array_equal(back.reshape((adim,) * 3)[sl], ref.reshape((adim,) * 3)[sl]))
+    del arr_in, arr_out, back, ref
+    # periodic ghost fill of the 512^3 + one-brick ghost domain
+    plan = B.GhostPlan.periodic(grid, (n // 8,) * 3, (1, 1, 1))
+    out["ghost_fill"] = rate(2 * plan.n * 512 * 8, timed(lambda: B.ghostFill(plan, brick, sp)))
+    out["ghost_fill"]["ghost_bricks"] = plan.n
+    del st, brick, dinfo, plan
+    # BrickDecomp of the same domain (skin3d_good), its periodic exchange
+    dec = D.BrickDecomp([n] * 3, gz, (8, 8, 8), numfield=1)
+    dec.initialize(D.SKIN3D_GOOD)
+    dst = B.BrickStorage.allocate_device(dec.nbricks, 512, f64)
+    links = dec.exchange_links(dst.ptr, 512 * 8)
+    out["decomp_exchange"] = rate(2 * int(links[:, 2].sum()), timed(lambda: dec.exchange(dst, sp)))
+    out["decomp_exchange"]["regions"] = dec.nregions
+    dec.close()
+    del dst
+    # 4-D 9-point star on 64^4 points (4^4 bricks, one ghost brick per side)
+    n4 = 64
+    gb4 = n4 // 4 + 2
+    grid4, adj4 = B4.init_grid([gb4] * 4)
+    adj_dev = B.DeviceBuffer(adj4.nbytes)
+    adj_dev.upload(np.ascontiguousarray(adj4))
+    g4 = grid4.reshape((gb4,) * 4)
+    inner = B.BrickList(np.ascontiguousarray(g4[1:-1, 1:-1, 1:-1, 1:-1].reshape(-1)))
+    st4 = B4.mpi9pt()
+    out["sweep4_mpi9pt"] = {"points": n4 ** 4}
+    for name, dt in (("f64", f64), ("f32", _abi.BK_F32)):
+        s4 = B.BrickStorage.allocate_device(len(grid4), 512, dt)
+        call("bk_fill_uniform", C.c_void_p(s4.ptr), len(grid4) * 512, dt, 5, -1.0, 1.0, sp)
+        sec = timed(lambda: B4.sweep4(adj_dev, len(grid4), s4, 0, 256, inner, st4, stream=sp))
+        r = rate(2 * B.ELEM_SIZE[dt] * n4 ** 4, sec)
+        r["gstencil_s"] = round(n4 ** 4 / sec / 1e9, 2)
+        out["sweep4_mpi9pt"][name] = r
+        del s4
+    assert B.error_flags() == 0
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -633,5 +734,7 @@ if __name__ == "__main__":
         run_batched(a)
     elif a.form == "serving":
         run_serving(a)
+    elif a.form == "next":
+        run_next(a)
     else:
         run_ours(a)

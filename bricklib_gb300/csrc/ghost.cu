@@ -3,12 +3,41 @@
 
 namespace bk {
 
-// One CTA per (dst, src) brick pair; `words` words of W bytes per brick field.
+// (dst, src) brick pairs; `words` words of W bytes per brick field.  Bricks of at most 256
+// words: a CTA takes GF_PAIRS pairs at a time, each thread loading its word of every pair
+// before storing any (more bytes in flight per SM); larger bricks: one pair per CTA step.
+constexpr int GF_PAIRS = 4;
 template <typename W>
 __global__ void __launch_bounds__(256)
 ghost_fill_kernel(const unsigned *__restrict__ pairs, unsigned npairs, unsigned char *dat,
                   unsigned long long step_bytes, unsigned long long off_bytes, unsigned words,
                   long long chunks, int *err) {
+  if (words <= blockDim.x) {
+    const unsigned t = threadIdx.x;
+    for (unsigned p0 = blockIdx.x * GF_PAIRS; p0 < npairs; p0 += gridDim.x * GF_PAIRS) {
+      W v[GF_PAIRS];
+      W *d[GF_PAIRS];
+#pragma unroll
+      for (int q = 0; q < GF_PAIRS; ++q) {
+        d[q] = nullptr;
+        const unsigned p = p0 + q;
+        if (p >= npairs) continue;
+        const unsigned dst = pairs[2 * p], src = pairs[2 * p + 1];
+        if ((long long)dst >= chunks || (long long)src >= chunks) {
+          if (t == 0) atomicOr(err, FLAG_BOUNDS);
+          continue;
+        }
+        if (t < words) {
+          v[q] = reinterpret_cast<const W *>(dat + (size_t)src * step_bytes + off_bytes)[t];
+          d[q] = reinterpret_cast<W *>(dat + (size_t)dst * step_bytes + off_bytes) + t;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < GF_PAIRS; ++q)
+        if (d[q]) *d[q] = v[q];
+    }
+    return;
+  }
   for (unsigned p = blockIdx.x; p < npairs; p += gridDim.x) {
     const unsigned dst = pairs[2 * p], src = pairs[2 * p + 1];
     if ((long long)dst >= chunks || (long long)src >= chunks) {
@@ -31,7 +60,16 @@ __global__ void __launch_bounds__(256) region_copy_kernel(const uint64_t *__rest
     if (((from | to | bytes) & 15) == 0) {
       const uint4 *s = reinterpret_cast<const uint4 *>(from);
       uint4 *d = reinterpret_cast<uint4 *>(to);
-      for (uint64_t w = t; w < bytes / 16; w += nt) d[w] = s[w];
+      const uint64_t n = bytes / 16;
+      uint64_t w = t;
+      for (; w + 3 * nt < n; w += 4 * nt) {  // four loads in flight before the stores
+        const uint4 a = s[w], b = s[w + nt], c = s[w + 2 * nt], e = s[w + 3 * nt];
+        d[w] = a;
+        d[w + nt] = b;
+        d[w + 2 * nt] = c;
+        d[w + 3 * nt] = e;
+      }
+      for (; w < n; w += nt) d[w] = s[w];
     } else {
       const uint64_t *s = reinterpret_cast<const uint64_t *>(from);
       uint64_t *d = reinterpret_cast<uint64_t *>(to);
@@ -48,7 +86,8 @@ int ghost_fill(const unsigned *pairs, unsigned npairs, const bk_field *f, const 
   const unsigned long long step_b = f->step * es, off_b = f->offset * es;
   const size_t bytes = (size_t)L.size() * es;
   const uintptr_t base = reinterpret_cast<uintptr_t>(f->dat);
-  const unsigned grid = npairs < (1u << 30) ? npairs : (1u << 30);
+  const unsigned groups = (npairs + GF_PAIRS - 1) / GF_PAIRS;
+  const unsigned grid = groups < (1u << 30) ? groups : (1u << 30);
   unsigned char *dat = reinterpret_cast<unsigned char *>(f->dat);
   if (((base | step_b | off_b | bytes) & 15) == 0)
     ghost_fill_kernel<uint4><<<grid, 256, 0, s>>>(pairs, npairs, dat, step_b, off_b, (unsigned)(bytes / 16), f->chunks, err);
