@@ -1,8 +1,9 @@
 // Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
 // tap list, e.g. the 9-point star of stencils/mpi9pt.py.  One CTA of 256 threads computes one
 // listed brick at a time: it stages the 81 adjacency entries, gathers the (4+2R)^4
-// neighbourhood into shared memory (converted once to the arithmetic type), and each thread
-// computes one element.  Out-of-range list or adjacency entries are clamped / skipped and
+// neighbourhood into shared memory (converted once to the arithmetic type; the source slot and
+// in-brick offset of every tile element come from a table the CTA builds once), and each
+// thread computes one element.  Out-of-range list or adjacency entries are clamped / skipped and
 // raise the device error flag, as in the 3-D kernels.
 #include "bk_common.cuh"
 
@@ -36,6 +37,21 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
   __shared__ AT tile[TILE];
   __shared__ unsigned nbr[81];
   __shared__ unsigned cur;
+  // where every tile element comes from (adjacency slot, offset in that brick): fixed by the
+  // layout, so computed once per CTA instead of per brick
+  __shared__ unsigned short toffs[TILE];
+  __shared__ unsigned char tslot[TILE];
+  for (int e = threadIdx.x; e < TILE; e += blockDim.x) {
+    int r = e;
+    const int ii = r % E; r /= E;
+    const int jj = r % E; r /= E;
+    const int kk = r % E;
+    const int ll = r / E;
+    const int ql = ll < R ? -1 : (ll >= R + B ? 1 : 0), qk = kk < R ? -1 : (kk >= R + B ? 1 : 0);
+    const int qj = jj < R ? -1 : (jj >= R + B ? 1 : 0), qi = ii < R ? -1 : (ii >= R + B ? 1 : 0);
+    tslot[e] = (unsigned char)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
+    toffs[e] = (unsigned short)L.offset(ll - R - ql * B, kk - R - qk * B, jj - R - qj * B, ii - R - qi * B);
+  }
   for (unsigned n = blockIdx.x; n < nlist; n += gridDim.x) {
     if (threadIdx.x == 0) {
       unsigned b = blist[n];
@@ -60,18 +76,8 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     }
     __syncthreads();
     if (b != 0xFFFFFFFFu && nbr[40] != 0xFFFFFFFFu) {
-      for (int e = threadIdx.x; e < TILE; e += blockDim.x) {
-        int r = e;
-        const int ii = r % E; r /= E;
-        const int jj = r % E; r /= E;
-        const int kk = r % E;
-        const int ll = r / E;
-        const int ql = ll < R ? -1 : (ll >= R + B ? 1 : 0), qk = kk < R ? -1 : (kk >= R + B ? 1 : 0);
-        const int qj = jj < R ? -1 : (jj >= R + B ? 1 : 0), qi = ii < R ? -1 : (ii >= R + B ? 1 : 0);
-        const unsigned src = nbr[((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1)];
-        const int o = L.offset(ll - R - ql * B, kk - R - qk * B, jj - R - qj * B, ii - R - qi * B);
-        tile[e] = (AT)Elem<T>::load(in + (size_t)src * in_step + o);
-      }
+      for (int e = threadIdx.x; e < TILE; e += blockDim.x)
+        tile[e] = (AT)Elem<T>::load(in + (size_t)nbr[tslot[e]] * in_step + toffs[e]);
     }
     __syncthreads();
     if (b != 0xFFFFFFFFu && nbr[40] != 0xFFFFFFFFu && threadIdx.x < B * B * B * B) {
@@ -95,8 +101,17 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
 template <typename T, typename AT, int R>
 static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
                    unsigned nlist, const Layout4 &L, const Taps4 &tp, int *err, cudaStream_t s) {
-  long long grid = nlist < (1u << 30) ? nlist : (1u << 30);
-  sweep4_kernel<T, AT, R><<<(unsigned)grid, 256, 0, s>>>(
+  // persistent CTAs (each builds its tile table once): as many as fit on the GPU
+  auto kern = sweep4_kernel<T, AT, R>;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e0 == cudaSuccess) e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "sweep4 launch setup");
+  long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
+  if (grid > nlist) grid = nlist;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, 256, 0, s>>>(
       adj, nbricks, reinterpret_cast<const T *>(in->dat) + in->offset, in->step, in->chunks,
       reinterpret_cast<T *>(out->dat) + out->offset, out->step, out->chunks, blist, nlist, L, tp, err);
   cudaError_t e = cudaGetLastError();
