@@ -1,9 +1,8 @@
 // Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
-// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  One CTA of 256 threads computes one
-// listed brick at a time: it stages the 81 adjacency entries, gathers the (4+2R)^4
-// neighbourhood into shared memory (converted once to the arithmetic type; the source slot and
-// in-brick offset of every tile element come from a table the CTA builds once), and each
-// thread computes one element.  Out-of-range list or adjacency entries are clamped / skipped and
+// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 256 threads: a
+// brick's (4+2R)^4 neighbourhood is gathered into shared memory by asynchronous copies (the
+// source slot and in-brick offset of every tile element from a table the CTA builds once)
+// while the previous brick is computed, one element per thread.  Out-of-range list or adjacency entries are clamped / skipped and
 // raise the device error flag, as in the 3-D kernels.
 #include "bk_common.cuh"
 
@@ -28,20 +27,36 @@ struct Taps4 {
   float cf[BK_MAX_TAPS4];
 };
 
+// Element copy global -> shared through the asynchronous copy path (4 or 8 bytes).
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(unsigned dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit4() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait4() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Persistent CTAs walk the brick list with a stride of the grid, pipelined: while brick j is
+// computed from one tile buffer, brick j+1's neighbourhood is gathered into the other by
+// asynchronous copies, and brick j+2's list and adjacency entries are staged (three
+// adjacency slots, so no slot is rewritten while read).  Two block barriers per brick.
 template <typename T, typename AT, int R>
 __global__ void __launch_bounds__(256)
 sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__restrict__ in, unsigned long long in_step,
               long long in_chunks, T *__restrict__ out, unsigned long long out_step, long long out_chunks,
               const unsigned *__restrict__ blist, unsigned nlist, const Layout4 L, const Taps4 tp, int *err) {
+  static_assert(sizeof(T) == sizeof(AT) && (sizeof(T) == 4 || sizeof(T) == 8), "the tile holds the storage type");
   constexpr int B = 4, E = B + 2 * R, TILE = E * E * E * E;
-  __shared__ AT tile[TILE];
-  __shared__ unsigned nbr[81];
-  __shared__ unsigned cur;
-  // where every tile element comes from (adjacency slot, offset in that brick): fixed by the
-  // layout, so computed once per CTA instead of per brick
-  __shared__ unsigned short toffs[TILE];
-  __shared__ unsigned char tslot[TILE];
-  for (int e = threadIdx.x; e < TILE; e += blockDim.x) {
+  constexpr unsigned NONE = 0xFFFFFFFFu;
+  // dynamic shared memory: tile[2][TILE], then where every tile element comes from (offset in
+  // its brick, adjacency slot): fixed by the layout, so computed once per CTA
+  extern __shared__ __align__(16) unsigned char smem4[];
+  T(*tile)[TILE] = reinterpret_cast<T(*)[TILE]>(smem4);
+  unsigned short *toffs = reinterpret_cast<unsigned short *>(smem4 + 2 * TILE * sizeof(T));
+  unsigned char *tslot = reinterpret_cast<unsigned char *>(toffs + TILE);
+  __shared__ unsigned nbr[3][81];
+  const int t = threadIdx.x;
+  for (int e = t; e < TILE; e += blockDim.x) {
     int r = e;
     const int ii = r % E; r /= E;
     const int jj = r % E; r /= E;
@@ -52,38 +67,60 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     tslot[e] = (unsigned char)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
     toffs[e] = (unsigned short)L.offset(ll - R - ql * B, kk - R - qk * B, jj - R - qj * B, ii - R - qi * B);
   }
-  for (unsigned n = blockIdx.x; n < nlist; n += gridDim.x) {
-    if (threadIdx.x == 0) {
-      unsigned b = blist[n];
-      if (b >= nbricks) {
+  const unsigned long long gs = gridDim.x;
+  // this thread's adjacency entry (slot t < 81) of list entry n; slot 40 carries NONE for a
+  // brick that is not computed (past the list, or out of range: flagged)
+  auto fetch = [&](unsigned long long n) -> unsigned {
+    if (t >= 81) return 0u;
+    if (n >= nlist) return t == 40 ? NONE : 0u;
+    const unsigned b = blist[n];
+    if (b >= nbricks) {
+      if (t == 40) {
         atomicOr(err, FLAG_BOUNDS);
-        b = 0xFFFFFFFFu;
+        return NONE;
       }
-      cur = b;
+      return 0u;
     }
-    __syncthreads();
-    const unsigned b = cur;
-    if (b != 0xFFFFFFFFu) {
-      for (int s = threadIdx.x; s < 81; s += blockDim.x) {
-        unsigned v = adj[(size_t)b * 81 + s];
-        const bool bad = (long long)v >= in_chunks || (s == 40 && (long long)v >= out_chunks);
-        if (bad) {
-          atomicOr(err, FLAG_BOUNDS);
-          v = s == 40 ? 0xFFFFFFFFu : 0u;
-        }
-        nbr[s] = v;
-      }
+    unsigned v = adj[(size_t)b * 81 + t];
+    if ((long long)v >= in_chunks || (t == 40 && (long long)v >= out_chunks)) {
+      atomicOr(err, FLAG_BOUNDS);
+      v = t == 40 ? NONE : 0u;
     }
-    __syncthreads();
-    if (b != 0xFFFFFFFFu && nbr[40] != 0xFFFFFFFFu) {
-      for (int e = threadIdx.x; e < TILE; e += blockDim.x)
-        tile[e] = (AT)Elem<T>::load(in + (size_t)nbr[tslot[e]] * in_step + toffs[e]);
+    return v;
+  };
+  auto issue = [&](int slot, int buf) {
+    const unsigned *nb = nbr[slot];
+    if (nb[40] != NONE) {
+      const unsigned base = (unsigned)__cvta_generic_to_shared(&tile[buf][0]);
+      for (int e = t; e < TILE; e += blockDim.x)
+        cp_async_elem<sizeof(T)>(base + e * (unsigned)sizeof(T), in + (size_t)nb[tslot[e]] * in_step + toffs[e]);
     }
-    __syncthreads();
-    if (b != 0xFFFFFFFFu && nbr[40] != 0xFFFFFFFFu && threadIdx.x < B * B * B * B) {
-      const int t = threadIdx.x;
-      const int i = t % B, j = (t / B) % B, k = (t / (B * B)) % B, l = t / (B * B * B);
-      const AT *c = tile + (((l + R) * E + (k + R)) * E + (j + R)) * E + (i + R);
+    cp_async_commit4();
+  };
+  const unsigned long long n0 = blockIdx.x;
+  {
+    const unsigned a0 = fetch(n0), a1 = fetch(n0 + gs);
+    if (t < 81) {
+      nbr[0][t] = a0;
+      nbr[1][t] = a1;
+    }
+  }
+  unsigned ahead = fetch(n0 + 2 * gs);
+  __syncthreads();  // tables and the first two adjacency slots
+  issue(0, 0);
+  int j = 0;
+  for (unsigned long long n = n0; n < nlist; n += gs, ++j) {
+    const int cur = j % 3, nxt = (j + 1) % 3, far = (j + 2) % 3, buf = j & 1;
+    __syncthreads();  // the previous brick's compute is done with tile[buf ^ 1] and slot far
+    issue(nxt, buf ^ 1);
+    if (t < 81) nbr[far][t] = ahead;
+    ahead = fetch(n + 3 * gs);
+    cp_async_wait4<1>();  // this thread's copies for brick n have landed
+    __syncthreads();      // ... and everybody else's
+    const unsigned ob = nbr[cur][40];
+    if (ob != NONE && t < B * B * B * B) {
+      const int i = t % B, jj = (t / B) % B, k = (t / (B * B)) % B, l = t / (B * B * B);
+      const T *c = tile[buf] + (((l + R) * E + (k + R)) * E + (jj + R)) * E + (i + R);
       AT v;
       if constexpr (sizeof(AT) == 8) {
         v = tp.c[0] * c[tp.toff[0]];
@@ -92,10 +129,10 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
         v = tp.cf[0] * c[tp.toff[0]];
         for (int q = 1; q < tp.n; ++q) v = fmaf(tp.cf[q], c[tp.toff[q]], v);
       }
-      Elem<T>::store(out + (size_t)nbr[40] * out_step + L.offset(l, k, j, i), v);
+      Elem<T>::store(out + (size_t)ob * out_step + L.offset(l, k, jj, i), v);
     }
-    __syncthreads();
   }
+  cp_async_wait4<0>();  // no copy may outlive the kernel
 }
 
 template <typename T, typename AT, int R>
@@ -103,15 +140,18 @@ static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, co
                    unsigned nlist, const Layout4 &L, const Taps4 &tp, int *err, cudaStream_t s) {
   // persistent CTAs (each builds its tile table once): as many as fit on the GPU
   auto kern = sweep4_kernel<T, AT, R>;
+  constexpr int E = 4 + 2 * R, TILE = E * E * E * E;
+  constexpr size_t smem = 2 * TILE * sizeof(T) + TILE * 3;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e0 = cudaGetDevice(&dev);
   if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e0 == cudaSuccess) e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0);
+  if (e0 == cudaSuccess && smem > 48 * 1024) e0 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e0 == cudaSuccess) e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
   if (e0 != cudaSuccess) return cuda_fail(e0, "sweep4 launch setup");
   long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
   if (grid > nlist) grid = nlist;
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, 256, 0, s>>>(
+  kern<<<(unsigned)grid, 256, smem, s>>>(
       adj, nbricks, reinterpret_cast<const T *>(in->dat) + in->offset, in->step, in->chunks,
       reinterpret_cast<T *>(out->dat) + out->offset, out->step, out->chunks, blist, nlist, L, tp, err);
   cudaError_t e = cudaGetLastError();
