@@ -129,6 +129,7 @@ SIGNATURES = {
     "bk_batch_set_grid": (C.c_int, [_vp, C.c_int]),
     "bk_batch_run": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp]),
     "bk_batch_parity": (C.c_int, [_vp]),
+    "bk_batch_is_arena": (C.c_int, [_vp]),
     "bk_batch_destroy": (C.c_int, [_vp]),
     "bk_copy_to_bricks": (C.c_int, [_vp, _P(C.c_long), _P(C.c_long), _P(C.c_long), _vp, _P(bk_field),
                                     _P(bk_layout), _vp]),

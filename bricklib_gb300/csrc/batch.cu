@@ -375,9 +375,14 @@ static int batch_arena(bk_batch *b, const bk_batch_domain *doms, unsigned ndom, 
   std::sort(sorted.begin(), sorted.end());
   for (unsigned d = 1; d < ndom; ++d)
     if (sorted[d].first < sorted[d - 1].second) return BK_OK;  // overlapping domains
-  unsigned long long total = 0;
-  for (const auto &r : ranges) total = std::max(total, r.second);
-  if (total > 0x7FFFFFFFull) return BK_OK;
+  unsigned long long total = 0, sum = 0;
+  for (const auto &r : ranges) {
+    total = std::max(total, r.second);
+    sum += r.second - r.first;
+  }
+  // the ranges must tile the arena exactly (separate allocations that merely happen to be
+  // step-aligned would leave gaps the global tables would span)
+  if (total != sum || total > 0x7FFFFFFFull) return BK_OK;
   // host lists: global work per stencil, global fill pairs
   std::vector<std::vector<unsigned>> per_st(nst);
   std::vector<unsigned> gpairs;
@@ -561,6 +566,8 @@ int bk_batch_run(bk_batch *b, int steps, int fill_every, int use_graph, void *st
 }
 
 int bk_batch_parity(const bk_batch *b) { return b ? b->parity : -1; }
+
+int bk_batch_is_arena(const bk_batch *b) { return b ? (b->arena ? 1 : 0) : -1; }
 
 int bk_batch_destroy(bk_batch *b) {
   if (!b) return BK_OK;

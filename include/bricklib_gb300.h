@@ -358,22 +358,29 @@ typedef struct bk_batch_domain {
 
 typedef struct bk_batch bk_batch;
 
-/* Build a batch: domains share one layout, one storage type (FP64 or FP32) and one
- * accumulation mode; up to 8 stencils, any that bk_sweep accepts.  Builds on the device the
- * global (domain, brick) work list, sorted by stencil, and the (domain, dst, src) fill list.
- * Field 0 (off0) holds the input of the first step. */
+/* Build a batch: domains share one layout, one storage type and one accumulation mode; up to
+ * 8 stencils, any that bk_sweep accepts.  Builds on the device the global (domain, brick) work
+ * list, sorted by stencil, and the (domain, dst, src) fill list.  When the domains' storages
+ * are brick ranges of one storage (same step and field offsets, ranges tiling it), the batch
+ * is one brick set instead: a global adjacency (each domain's entries shifted by its first
+ * brick), global work and fill lists, and steps of plain bk_sweep / bk_ghost_fill calls.
+ * Per-domain storages take FP64 or FP32.  Field 0 (off0) holds the input of the first step. */
 int bk_batch_create(bk_batch **batch, const bk_batch_domain *doms, unsigned ndom, const bk_stencil *stencils,
                     unsigned nstencils, const bk_layout *lay, int dtype, int acc);
 /* Cap the number of CTAs of the persistent sweep launch (0 = one CTA per work group);
  * the autotuner's block-count knob. */
 int bk_batch_set_grid(bk_batch *batch, int max_ctas);
 /* Advance every domain `steps` steps: before every `fill_every`-th step (0 = never) the ghost
- * plans are applied to the current input fields, then one persistent launch sweeps the whole
- * work list.  With use_graph the sequence is captured once per (steps, fill_every, parity)
- * into a CUDA graph kept by the batch and replayed on later calls. */
+ * plans are applied to the current input fields, then one launch per stencil sweeps that
+ * stencil's segment of the work list.  With use_graph the sequence is captured once per
+ * (steps, fill_every, parity) into a CUDA graph kept by the batch and replayed on later calls. */
 int bk_batch_run(bk_batch *batch, int steps, int fill_every, int use_graph, void *stream);
 /* Which field (0 or 1) holds the newest values. */
 int bk_batch_parity(const bk_batch *batch);
+/* 1 when the batch's domains are brick ranges of one storage (a common brick step, ranges
+ * tiling it without gaps) and the batch therefore runs as one brick set through the plain
+ * sweep kernels; 0 for domains in storages of their own; -1 for NULL. */
+int bk_batch_is_arena(const bk_batch *batch);
 /* Synchronises the device and releases the batch's device memory and graphs; the domains'
  * storages belong to the caller. */
 int bk_batch_destroy(bk_batch *batch);

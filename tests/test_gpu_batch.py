@@ -172,8 +172,10 @@ def test_arena_batch_equals_per_domain_storages(wrap):
     same interiors bit for bit, with the boundary in the adjacency and with ghost fills."""
     w = small_workload(nd=8)
     res = []
+    from bricklib_gb300 import _abi
     for arena in (True, False):
         b = BT.Batch(w, B.Layout(), BK_F32, wrap=wrap, arena=arena)
+        assert _abi.lib().bk_batch_is_arena(b.h) == (1 if arena else 0)
         b.run(5)
         B.synchronize()
         assert B.error_flags() == 0
