@@ -532,7 +532,7 @@ def run_precision(args):
 
 
 def run_batched(args):
-    """The batched form (BASELINE config 4): autotune the layout, then 10 FP32 steps of all 256
+    """The batched form (256 uneven periodic FP32 domains): autotune the layout, then 10 FP32 steps of all 256
     domains from one captured graph, against the plain FP64 drop-in run domain by domain (and
     an unbatched FP32 run), with the FP32 error against FP64."""
     import torch
@@ -604,7 +604,7 @@ def run_batched(args):
 
 
 def run_serving(args):
-    """The serving form (BASELINE config 5): Poisson arrivals of the mixed job set at each rate
+    """The serving form (mixed FP64 / FP32 jobs of up to 256^3): Poisson arrivals of the mixed job set at each rate
     against the continuous-batching server; p50 / p99 latency and aggregate GStencil/s."""
     import torch
     from bricklib_gb300 import _abi, serving

@@ -152,7 +152,7 @@ static int plan_sweep(const bk_field *in, const bk_field *out, const bk_stencil 
   else if (acc == BK_ACC_COMPENSATED) return fail(BK_ERR_UNSUPPORTED, "compensated accumulation is for FP32 / BF16 storage");
   else if (acc == BK_ACC_FLOATFLOAT && in->dtype == BK_F64) plan->acc = ACCM_FF;
   else if (acc == BK_ACC_FLOATFLOAT) return fail(BK_ERR_UNSUPPORTED, "float-float arithmetic is for FP64 storage");
-  else return fail(BK_ERR_UNSUPPORTED, "accumulation mode not available in this build");
+  else return fail(BK_ERR_UNSUPPORTED, "accumulation mode not available");
   // the pipelined kernel copies whole 16-byte (or brick-row) vectors: it needs a row-major
   // layout and vector-aligned input addresses
   {

@@ -8,7 +8,7 @@
 namespace bk {
 
 // cuTensorMapEncodeTiled, looked up through the runtime so that the library does not link
-// the driver library directly (it loads on machines without a GPU driver).
+// the CUDA driver library directly (it loads on machines without a GPU driver).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);

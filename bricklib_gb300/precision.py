@@ -2,7 +2,7 @@
 accumulation, compensated for the 125-point cube), with the error of every lower-precision
 run measured on the device in FP64 against the FP64 run.
 
-Problem (BASELINE config 3): a periodic n^3 interior with an 8-cell ghost zone, initial
+Problem: a periodic n^3 interior with an 8-cell ghost zone, initial
 field = sum of 8 seeded random-phase sines + 1e-3 uniform noise (bk_fill_sines); the
 7-point explicit heat step (centre 0.4, axes 0.1 = dt*alpha/h^2, stencils/mpi7pt.py with
 fake.h:11-12) and the 125-point cube; ghost bricks refreshed from the periodic plan before

@@ -1,5 +1,5 @@
-"""Serving form: Python client of the continuous-batching server (bk_server_*), the job mix
-of BASELINE config 5 and a Poisson load generator.
+"""Serving form: Python client of the continuous-batching server (bk_server_*), the mixed
+job set and a Poisson load generator.
 
 Jobs: a periodic domain drawn as in the batched form (each edge log-uniform on [16, 192],
 rounded to a multiple of 8), a stencil from the five plain shapes, a step count uniform on

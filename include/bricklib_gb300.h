@@ -38,7 +38,7 @@ typedef enum bk_status {
   BK_ERR_ARG = 1,         /* invalid argument (message says which) */
   BK_ERR_CUDA = 2,        /* a CUDA runtime call failed */
   BK_ERR_NOMEM = 3,       /* device or host allocation failed */
-  BK_ERR_UNSUPPORTED = 4, /* valid request this build has no kernel for */
+  BK_ERR_UNSUPPORTED = 4, /* valid request the library has no kernel for */
   BK_ERR_BOUNDS = 5,      /* a kernel met an out-of-range brick index and skipped it */
   BK_ERR_BUDGET = 6,      /* serving: request exceeds the HBM budget */
   BK_ERR_STATE = 7,       /* call not valid in the object's current state */
