@@ -65,6 +65,16 @@ def make_workload(ndom: int = 256, seed: int = 4, lo: int = 16, hi: int = 192, m
     return Workload(doms, [stencils.make(s, seed) for s in shapes])
 
 
+def periodic_adjacency(adj: np.ndarray, pairs: np.ndarray) -> np.ndarray:
+    """The adjacency with the periodic boundary in it: every entry that names a ghost brick
+    (a `dst` of the periodic plan `pairs`) names the interior brick the fill copies into it
+    (its `src`) instead."""
+    src = np.arange(len(adj), dtype=np.uint32)
+    pairs = np.asarray(pairs, dtype=np.uint32).reshape(-1, 2)
+    src[pairs[:, 0]] = pairs[:, 1]
+    return np.ascontiguousarray(src[np.asarray(adj, dtype=np.uint32)])
+
+
 def layout_valid(w: Workload, lay: B.Layout) -> bool:
     return all(d.n[a] % lay.bdim[a] == 0 and d.n[a] >= lay.bdim[a] for d in w.domains for a in range(3))
 
@@ -93,9 +103,7 @@ class DomainStorage:
         self.interior = np.ascontiguousarray(g3[1:-1, 1:-1, 1:-1].reshape(-1))
         pairs = B.GhostPlan.periodic(self.grid, nb, (1, 1, 1)).host
         if wrap:
-            src = np.arange(self.nbricks, dtype=np.uint32)
-            src[pairs[:, 0]] = pairs[:, 1]
-            info = B.BrickInfo(self.nbricks, np.ascontiguousarray(src[info.adj]))
+            info = B.BrickInfo(self.nbricks, periodic_adjacency(info.adj, pairs))
             pairs = np.zeros((0, 2), dtype=np.uint32)
         self.wrap = wrap
         self.pairs = pairs

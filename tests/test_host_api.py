@@ -160,3 +160,34 @@ def test_cpp_headers_match_reference_accessor(tmp_path):
     adj = np.frombuffer(raw, dtype=np.uint32, count=60 * 27, offset=pos + 240)
     np.testing.assert_array_equal(grid, g["grid"])
     np.testing.assert_array_equal(adj, g["adj"])
+
+
+@pytest.mark.parametrize("nb", [(3, 4, 5), (1, 2, 3), (1, 1, 1)])
+def test_periodic_adjacency_points_at_wrapped_interior_bricks(nb):
+    """The batch's periodic adjacency (host side): every neighbour of an interior brick is the
+    interior brick at the wrapped position, and entries between interior bricks are unchanged
+    (one-brick-wide axes wrap onto the brick itself)."""
+    from bricklib_gb300 import batch as BT
+    g = tuple(x + 2 for x in nb)  # (k, j, i) bricks with one ghost brick per side
+    grid, info = B.init_grid(list(reversed(g)))
+    nb_c, gb_c = (C.c_long * 3)(*nb), (C.c_long * 3)(1, 1, 1)
+    cnt = C.c_long()
+    gr = np.ascontiguousarray(grid, dtype=np.uint32)
+    _abi.call("bk_periodic_plan", gr.ctypes.data_as(C.c_void_p), nb_c, gb_c, None, 0, C.byref(cnt))
+    pairs = np.empty((cnt.value, 2), dtype=np.uint32)
+    _abi.call("bk_periodic_plan", gr.ctypes.data_as(C.c_void_p), nb_c, gb_c, pairs.ctypes.data_as(C.c_void_p),
+              cnt.value, C.byref(cnt))
+    wadj = BT.periodic_adjacency(info.adj, pairs)
+    g3 = grid.reshape(g)
+    for k in range(1, g[0] - 1):
+        for j in range(1, g[1] - 1):
+            for i in range(1, g[2] - 1):
+                b = g3[k, j, i]
+                for s in range(27):
+                    dk, dj, di = s // 9 - 1, (s // 3) % 3 - 1, s % 3 - 1
+                    wk = 1 + (k + dk - 1) % nb[0]
+                    wj = 1 + (j + dj - 1) % nb[1]
+                    wi = 1 + (i + di - 1) % nb[2]
+                    assert wadj[b, s] == g3[wk, wj, wi], (b, s)
+                    if 1 <= k + dk <= nb[0] and 1 <= j + dj <= nb[1] and 1 <= i + di <= nb[2]:
+                        assert wadj[b, s] == info.adj[b, s]
