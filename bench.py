@@ -406,7 +406,9 @@ def fp_instructions_per_point(st, acc, dtype=None) -> float:
     """Floating-point instructions per point of the kernel that runs `st` (native arithmetic on
     8x8x8 row-major bricks): a multiply-add per tap, except mirror-symmetric cubes, which the
     pipelined kernel evaluates from pair sums (sweep2_kernel.cuh, FAM_CUBESYM); for FP64
-    storage it also shares the row sums of a column pair (sym_cube_pair_shared)."""
+    storage it streams columns along i (sym_cube_istream: per column the class sums of both
+    rows of a lane, one multiply-add per class and i distance, 2R adds for the i taps; fewer
+    classes when the coefficients are also symmetric under k <-> j), counted in long runs."""
     from bricklib_gb300 import _abi
     taps = [tuple(t) for t in st.taps]
     r = st.radius
@@ -418,7 +420,8 @@ def fp_instructions_per_point(st, acc, dtype=None) -> float:
         return float(len(taps))
     ij = all(c[(k, j, i)] == c[(k, i, j)] for (k, j, i) in taps)
     if dtype == _abi.BK_F64:
-        return {(1, False): 17.0, (1, True): 15.25, (2, False): 63.0, (2, True): 52.5}[(r, ij)]
+        kj = all(c[(k, j, i)] == c[(j, k, i)] for (k, j, i) in taps)
+        return {(1, False): 14.0, (1, True): 13.0, (2, False): 43.0, (2, True): 37.0}[(r, kj)]
     return {(1, False): 18.25, (1, True): 16.5, (2, False): 69.0, (2, True): 58.5}[(r, ij)]
 
 

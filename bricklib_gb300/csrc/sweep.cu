@@ -101,6 +101,7 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   plan->toff1 = toff1;
   // mirror symmetry of a cube in every axis: c(dk,dj,di) == c(|dk|,|dj|,|di|) exactly
   plan->sym = plan->symij = false;
+  tp->kj = 0;
   if (fam == FAM_CUBE) {
     const int w = 2 * r + 1;
     bool sym = true;
@@ -124,6 +125,11 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
         for (int aj = 0; aj <= r; ++aj)
           for (int ai = 0; ai <= r; ++ai) ij = ij && tp->c[sym_index(ak, aj, ai, r)] == tp->c[sym_index(ak, ai, aj, r)];
       plan->symij = ij;
+      bool kj = true;
+      for (int ak = 0; ak <= r; ++ak)
+        for (int aj = 0; aj <= r; ++aj)
+          for (int ai = 0; ai <= r; ++ai) kj = kj && tp->c[sym_index(ak, aj, ai, r)] == tp->c[sym_index(aj, ak, ai, r)];
+      tp->kj = kj;
     }
   }
   for (int t = 0; t < TAP_PAIRS; ++t) tp->cp[t] = make_float2(tp->cf[t], tp->cf[t]);
@@ -168,8 +174,18 @@ static int plan_sweep(const bk_field *in, const bk_field *out, const bk_stencil 
     if (plan->acc == ACCM_FF && ((plan->fam == FAM_CUBE && !(plan->sym && plan->shape == 0)) || plan->r >= 4) &&
         !getenv("BK_SWEEP_PIPELINED"))
       plan->v2 = false;
+    // the column-pair kernels (cubes on 8x8x8 bricks, the FP32 / BF16 star row kernel) store
+    // two adjacent outputs at once: every output brick must start on a two-element boundary
+    const char *obase = reinterpret_cast<const char *>(out->dat) + out->offset * es;
+    plan->out_pair = reinterpret_cast<uintptr_t>(obase) % (2 * es) == 0 && (out->step * es) % (2 * es) == 0;
+    if (plan->fam == FAM_CUBE && plan->shape == 0 && !plan->out_pair) plan->v2 = false;
     // star stencils on 8x8x8 row-major bricks: the TMA-fed kernel, unless a kernel is forced
     plan->tma = tma_eligible(*plan, in) && !getenv("BK_SWEEP_ONESHOT") && !getenv("BK_SWEEP_PIPELINED");
+    // FP64 mirror-symmetric cubes: the pipelined kernel streams columns along i (BK_SWEEP_ISTREAM=0:
+    // one brick at a time)
+    const char *ist = getenv("BK_SWEEP_ISTREAM");
+    plan->istream = plan->v2 && plan->sym && plan->shape == 0 && in->dtype == BK_F64 && plan->acc == ACCM_NATIVE &&
+                    !(ist && !strcmp(ist, "0"));
   }
   *Lout = L;
   return BK_OK;

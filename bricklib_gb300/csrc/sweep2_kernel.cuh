@@ -391,6 +391,95 @@ __device__ __forceinline__ void sym_cube_pair_shared(const T *rt, T *ob, const i
   }
 }
 
+// FP64 mirror-symmetric cubes streamed along i.  With the CTA walking a contiguous share of
+// the brick list, consecutive entries that are i-neighbours (the next brick's column of
+// i-lo neighbours is this brick's centre column, and its centre column this brick's i-hi
+// column) form one stream.  For each tile column ii a lane forms, for its rows (k0, j) and
+// (k0 + 1, j), the class sums Q(c, b) = sum of x(k +- c, j +- b, ii) (from the row sums
+// H_b(k') = x(k', j - b) + x(k', j + b), shared by both rows) and from them
+// W_a(ii) = sum over (c, b) of coef(c, b, a) Q(c, b), a = 0..R.  The output at column i is
+// W_0(i) + sum over a of (W_a(i - a) + W_a(i + a)).  The W of a brick's last 2R columns carry
+// over to the next brick of a stream, so a brick costs 8 columns instead of 8 + 2R: the
+// 125-point cube takes 43 FP64 operations per point, 37 when its coefficients are also
+// symmetric under k <-> j (Q(c, b) + Q(b, c) share one multiply-add).  Each W depends on one
+// input column only, so a brick's outputs are the same bits whether the W of its first 2R
+// columns were carried or computed from its own tile.  Output (k, j, i) is parked in the tile
+// at its own input position, whose column was consumed R steps earlier (the CTA is this one
+// warp), and the finished brick leaves in whole-warp 512-byte stores, which also suits an
+// output field in mapped host memory.
+template <typename C, int R, bool KJ>
+__device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const int lane, const Taps &tp,
+                                                 double (&W)[2][R + 1][2 * R + 1], const bool cont) {
+  constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP, NW = 2 * R + 1;
+  static_assert(R == 1 || R == 2, "cube radius");
+  const int k0 = 2 * (lane >> 3), j = lane & 7;
+  double *col = rt + (k0 + R) * SK + (j + R) * SJ;  // tile (brick k0, brick j, column 0)
+  // W_a of tile column ii for both rows, pushed into the window (newest at NW - 1)
+  auto column = [&](const int ii) {
+    double H[R + 1][2 * R + 2];  // H[b][q]: plane k0 - R + q
+#pragma unroll
+    for (int q = 0; q < 2 * R + 2; ++q) {
+      const double *p = col + (q - R) * SK + ii;
+      H[0][q] = p[0];
+#pragma unroll
+      for (int b = 1; b <= R; ++b) H[b][q] = p[-b * SJ] + p[b * SJ];
+    }
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      double Q[R + 1][R + 1];
+#pragma unroll
+      for (int b = 0; b <= R; ++b) {
+        Q[0][b] = H[b][R + o];
+#pragma unroll
+        for (int c = 1; c <= R; ++c) Q[c][b] = H[b][R + o - c] + H[b][R + o + c];
+      }
+      if constexpr (KJ) {
+#pragma unroll
+        for (int c = 1; c <= R; ++c)
+#pragma unroll
+          for (int b = 0; b < c; ++b) Q[c][b] += Q[b][c];
+      }
+#pragma unroll
+      for (int a = 0; a <= R; ++a) {
+        double w = 0.0;
+#pragma unroll
+        for (int c = 0; c <= R; ++c)
+#pragma unroll
+          for (int b = 0; b <= (KJ ? c : R); ++b) {
+            const double cf = tp.c[sym_index(c, b, a, R)];
+            w = (c == 0 && b == 0) ? cf * Q[0][0] : fma(cf, Q[c][b], w);
+          }
+#pragma unroll
+        for (int m = 0; m + 1 < NW; ++m) W[o][a][m] = W[o][a][m + 1];
+        W[o][a][NW - 1] = w;
+      }
+    }
+  };
+  if (!cont) {
+#pragma unroll
+    for (int ii = RP - R; ii < RP + R; ++ii) column(ii);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    column(RP + R + i);  // the window now ends at column i + R: output i is complete
+    __syncwarp();        // every lane is past column RP + i
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      double v = W[o][0][R];
+#pragma unroll
+      for (int a = 1; a <= R; ++a) v += W[o][a][R - a] + W[o][a][R + a];
+      col[o * SK + RP + i] = v;
+    }
+  }
+  __syncwarp();
+  // 64 outputs per store: lane l writes elements 2l, 2l + 1 of rows 8q .. 8q + 7
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int e = q * 64 + 2 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
+    st_pair(ob + e, ld_pair(rt + (k + R) * SK + (jj + R) * SJ + RP + i));
+  }
+}
+
 // One brick's outputs from its staged tile (the compute of sweep2_kernel): each of the BJ*BI
 // threads (lt) owns one (j, i) column, or, for the column-pair cubes, each of the BJ*BI/2
 // threads a pair of columns.
@@ -653,11 +742,15 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
   }
 }
 
-template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH>
+// IST: FP64 mirror-symmetric cubes streamed along i (sym_cube_istream): each CTA takes a
+// contiguous share of the list instead of every gridDim.x-th group.
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH, bool IST>
 __global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC>::NT)
 sweep2_kernel(const SweepArgs a, const Taps tp) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
   constexpr int TPB = C::TPB, NB = C::NB, EPT = C::EPT;
+  static_assert(!IST || (C::PAIR && C::ES == 8 && NB == 1 && !BATCH && (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ)),
+                "i-streaming is for FP64 mirror-symmetric cubes, one brick per CTA, plain lists");
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
@@ -678,6 +771,10 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   }
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
+  // this CTA's groups: g0, g0 + gstride, ... below gend
+  const long long g0 = IST ? (long long)blockIdx.x * ngroups / gridDim.x : (long long)blockIdx.x;
+  const long long gend = IST ? ((long long)blockIdx.x + 1) * ngroups / gridDim.x : ngroups;
+  const long long gstride = IST ? 1 : (long long)gridDim.x;
 
   // Adjacency of a group: fetched into registers two groups ahead (its global-load latency
   // hides under the current group's compute), stored into one of three nbrs slots.
@@ -692,7 +789,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
       const int sl = lt + q * TPB;
       unsigned v = 0;
       int ok = 0;
-      if (sl < 27 && grp < ngroups && n < a.nlist) {
+      if (sl < 27 && grp < gend && n < a.nlist) {
         const unsigned *adj;
         unsigned b, nbricks;
         long long in_chunks, out_chunks;
@@ -774,20 +871,23 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   };
 
   // prologue: adjacency of the first two groups, copies of the first
-  long long grp = blockIdx.x;
+  long long grp = g0;
   fetch_adj(grp);
   store_adj(0);
-  fetch_adj(grp + gridDim.x);
+  fetch_adj(grp + gstride);
   store_adj(1);
   __syncthreads();
   issue(0, 0);
 
-  for (int it = 0; grp < ngroups; grp += gridDim.x, ++it) {
+  // i-streaming: W of the last 2R columns of the previous brick (sym_cube_istream)
+  double W[IST ? 2 : 1][IST ? R + 1 : 1][IST ? 2 * R + 1 : 1];
+
+  for (int it = 0; grp < gend; grp += gstride, ++it) {
     const int cur = it & 1, nxt = cur ^ 1;
     const int ncur = it % 3, nnxt = (it + 1) % 3, nfar = (it + 2) % 3;
     __syncthreads();     // nbrs[nnxt] visible; every thread is done with raw[nxt] and nbrs[nfar]
     issue(nxt, nnxt);
-    fetch_adj(grp + 2ll * gridDim.x);  // lands while this group computes
+    fetch_adj(grp + 2 * gstride);  // lands while this group computes
     cp_async_wait<1>();  // this thread's copies for the current group have landed
     __syncthreads();     // ... and everybody else's
 
@@ -801,7 +901,27 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
         for (int e = lt; e < C::TILE; e += TPB) ft[e] = split_f64(reinterpret_cast<const double *>(rt)[e]);
       __syncthreads();
     }
-    if (active) {
+    if constexpr (IST) {
+      // the stream continues when the previous group (list entry grp - 1, adjacency still in
+      // nbrs[nfar]) ran and its centre and i-hi columns of neighbours are this brick's i-lo
+      // and centre columns
+      const unsigned *prv = nbrs + nfar * 36;
+      bool same = true;
+      if (lt < 18) {
+        const int s9 = lt < 9 ? lt : lt - 9, sh = lt < 9 ? 0 : 1;
+        const int base = (s9 / 3) * 9 + (s9 % 3) * 3;  // (dk, dj) = (s9 / 3 - 1, s9 % 3 - 1), di = -1
+        same = nbr[base + sh] == prv[base + sh + 1];
+      }
+      const bool cont = __all_sync(0xFFFFFFFFu, same) && it > 0 && prv[27] != 0 && active;
+      if (active) {
+        T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
+        const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
+        T *ob = out + (size_t)nbr[13] * ostep;
+        double *tile = const_cast<double *>(rt);  // this warp's buffer until the next barrier
+        if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, tp, W, cont);
+        else sym_cube_istream<C, R, false>(tile, ob, lt, tp, W, cont);
+      }
+    } else if (active) {
       T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
       const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
       sweep2_brick<T, BK, BJ, BI, R, FAM, ACC>(rt, out + (size_t)nbr[13] * ostep, lt, tp);
@@ -811,12 +931,12 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   cp_async_wait<0>();  // no copy may outlive the kernel
 }
 
-template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH = false>
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH = false, bool IST = false>
 int launch_sweep2(const SweepArgs &a, const Taps &tp, cudaStream_t s, int grid_cap = 0) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
   static_assert(C::SMEM <= 227 * 1024, "tile too large");
   static_assert(BK * BJ * BI <= 8192 && C::TILE <= 16384, "plan entry fields overflow");
-  auto kern = sweep2_kernel<T, BK, BJ, BI, R, FAM, ACC, BATCH>;
+  auto kern = sweep2_kernel<T, BK, BJ, BI, R, FAM, ACC, BATCH, IST>;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -40,6 +40,10 @@ int sweep_dispatch_f64(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStr
   if (p.v2) {
     if (p.shape == 0) {
       // mirror-symmetric cubes: pair sums, fewer multiply-adds
+      if (p.sym && p.fam == FAM_CUBE && p.acc == ACCM_NATIVE && p.istream) {
+        if (p.r == 1) return launch_sweep2<double, 8, 8, 8, 1, FAM_CUBESYM, ACCM_NATIVE, false, true>(a, tp, s);
+        if (p.r == 2) return launch_sweep2<double, 8, 8, 8, 2, FAM_CUBESYM, ACCM_NATIVE, false, true>(a, tp, s);
+      }
       if (p.sym && p.fam == FAM_CUBE && p.acc == ACCM_NATIVE) {
         if (p.symij && p.r == 1) return launch_sweep2<double, 8, 8, 8, 1, FAM_CUBESYM_IJ, ACCM_NATIVE>(a, tp, s);
         if (p.symij && p.r == 2) return launch_sweep2<double, 8, 8, 8, 2, FAM_CUBESYM_IJ, ACCM_NATIVE>(a, tp, s);

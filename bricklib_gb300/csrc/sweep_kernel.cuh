@@ -72,6 +72,7 @@ struct Taps {
   float cl[BK_MAX_TAPS];   // float(c - cf): the low part, for float-float arithmetic
   double c[BK_MAX_TAPS];
   float2 cp[TAP_PAIRS];    // (cf, cf) of the first taps: operands of packed FP32 arithmetic
+  int kj;                  // mirror-symmetric cube also symmetric under the k <-> j swap
 };
 
 __host__ __device__ constexpr int sweep_threads(int tpb) { return tpb < 128 ? 128 : tpb; }
@@ -461,6 +462,8 @@ struct SweepPlan {
   bool sym;   // cube with mirror-symmetric coefficients (sym_index table filled)
   bool symij; // ... and symmetric under the i <-> j swap
   bool ops;   // pointwise pre / post operations (one-shot kernels only)
+  bool out_pair;  // every output brick starts on a boundary of two elements (pair stores)
+  bool istream;   // FP64 mirror-symmetric 8x8x8 cubes: columns streamed along i
   int fam;
   int r;
   int acc;

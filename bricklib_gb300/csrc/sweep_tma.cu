@@ -104,7 +104,7 @@ static bool narrow_iface(int dtype) {
 }
 
 bool tma_row(const SweepPlan &p) {
-  if (!p.tma || p.dtype == BK_F64 || p.acc == ACCM_FF) return false;
+  if (!p.tma || p.dtype == BK_F64 || p.acc == ACCM_FF || !p.out_pair) return false;
   const char *e = getenv("BK_TMA_ROW");
   return !(e && !strcmp(e, "0"));
 }

@@ -241,13 +241,15 @@ def test_out_of_range_adjacency_is_clamped_and_flagged():
     assert B.error_flags() == 0  # reading clears
 
 
-def _mirror_symmetric_cube(r, seed, ij=False):
+def _mirror_symmetric_cube(r, seed, ij=False, kj=False):
     """A (2r+1)^3 cube whose coefficient depends on (|dk|, |dj|, |di|) only; with `ij` also
-    symmetric under the swap of |dj| and |di|."""
+    symmetric under the swap of |dj| and |di|, with `kj` under the swap of |dk| and |dj|."""
     taps, _ = stencils.cube_taps(r)
     per = stencils.uniform01(seed, (r + 1) ** 3).reshape(r + 1, r + 1, r + 1)
     if ij:
         per = per + per.transpose(0, 2, 1)
+    if kj:
+        per = per + per.transpose(1, 0, 2)
     c = np.array([per[abs(t[0]), abs(t[1]), abs(t[2])] for t in taps])
     return stencils.custom(f"symcube{2 * r + 1}", taps, c / c.sum())
 
@@ -415,6 +417,106 @@ def test_row_kernel_bounds_are_flagged(monkeypatch):
         dom.download()
         outs.append(dom.storage.host.copy())
     np.testing.assert_array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
+
+
+def _istream_stencil(shape):
+    if shape == "cube125":
+        return stencils.make("cube125", 7)  # symmetric under every axis swap
+    r, ij, kj = {"sym27": (1, False, False), "sym27kj": (1, False, True),
+                 "sym125": (2, False, False), "sym125ij": (2, True, False)}[shape]
+    return _mirror_symmetric_cube(r, 50 + r, ij, kj)
+
+
+@pytest.mark.parametrize("shape", ["cube125", "sym27", "sym27kj", "sym125", "sym125ij"])
+def test_istream_cubes_same_bits_for_every_list_order(shape, monkeypatch):
+    """FP64 mirror-symmetric cubes carry per-column sums from one brick to the next along runs
+    of i-adjacent list entries.  Every list order -- grid order (long runs), shuffled (none),
+    grid-order pieces, repeated entries, a ragged tail -- writes the same bits into every
+    brick it lists; the result is within 1e-12 of the oracle and of the one-brick-at-a-time
+    kernel (BK_SWEEP_ISTREAM=0)."""
+    st = _istream_stencil(shape)
+    dom = GridDomain((32, 64, 128))  # (k, j, i): 4 x 8 x 16 interior bricks, runs of 16
+    arr = stencils.uniform(23, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    monkeypatch.delenv("BK_SWEEP_ISTREAM", raising=False)
+    assert B.sweepKernel(dom.brick(0), dom.brick(1), st) == "sweep2_kernel"
+    full = None
+    for key, lst in _row_lists(dom, 5).items():
+        got = _sweep_with(None, monkeypatch, dom, st, BK_ACC_NATIVE, B.BrickList(lst))
+        out = got.reshape(dom.nbricks, dom.nfields, -1)[:, 1, :]
+        if full is None:  # grid order: every interior brick
+            full = out.copy()
+            ok, md = mixed_ok(dom.interior_view(dom.get_field(1)), oracle_array(dom, arr, st))
+            assert ok, f"vs oracle: max |diff| {md}"
+        listed = np.unique(lst)
+        np.testing.assert_array_equal(out[listed].view(np.uint64), full[listed].view(np.uint64), err_msg=key)
+        assert int(np.count_nonzero((out.view(np.uint64) != np.uint64(0xFFFFFFFFFFFFFFFF)).any(axis=1))) == len(listed)
+    monkeypatch.setenv("BK_SWEEP_ISTREAM", "0")
+    got = _sweep_with(None, monkeypatch, dom, st, BK_ACC_NATIVE, dom.dev_interior)
+    ok, md = mixed_ok(got.reshape(dom.nbricks, dom.nfields, -1)[dom.interior, 1, :], full[dom.interior])
+    assert ok, f"vs one brick at a time: max |diff| {md}"
+
+
+def test_istream_follows_asymmetric_adjacency(monkeypatch):
+    """A run continues only where the next entry's i-lo and centre columns of neighbours are
+    this entry's centre and i-hi columns.  With i-lo, diagonal and i-hi entries re-pointed
+    (and bricks whose i neighbours are themselves) the streamed sweep reads exactly the
+    adjacency the one-brick-at-a-time kernel reads."""
+    st = stencils.make("cube125", 11)
+    dom = GridDomain((32, 64, 64), device=False)
+    adj = dom.bInfo.adj.copy()
+    rng = np.random.default_rng(12)
+    it = dom.interior
+    # slots (dk, dj, di): 12 (0, 0, -1), 3 (-1, 0, -1), 23 (+1, 0, +1), 11 (0, -1, +1), 14 (0, 0, +1)
+    for slot, frac in ((12, 5), (3, 6), (23, 6), (11, 7), (14, 9)):
+        v = rng.choice(it, size=len(it) // frac, replace=False)
+        adj[v, slot] = rng.choice(it, size=len(v))
+    selfies = rng.choice(it, size=len(it) // 7, replace=False)
+    adj[selfies, 14] = selfies
+    adj[selfies[::2], 12] = selfies[::2]
+    dom.bInfo = B.BrickInfo(dom.nbricks, adj)
+    arr = stencils.uniform(8, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.to_device()
+    dl = B.BrickList(np.concatenate([it, np.repeat(selfies[:50], 2)]).astype(np.uint32))
+    monkeypatch.delenv("BK_SWEEP_ISTREAM", raising=False)
+    streamed = _sweep_with(None, monkeypatch, dom, st, BK_ACC_NATIVE, dl)
+    monkeypatch.setenv("BK_SWEEP_ISTREAM", "0")
+    per_brick = _sweep_with(None, monkeypatch, dom, st, BK_ACC_NATIVE, dl)
+    a = streamed.reshape(dom.nbricks, dom.nfields, -1)[it, 1, :]
+    b = per_brick.reshape(dom.nbricks, dom.nfields, -1)[it, 1, :]
+    ok, md = mixed_ok(a, b)
+    assert ok, f"max |diff| {md}"
+
+
+@pytest.mark.parametrize("dtype,name", [(BK_F64, "cube125"), (BK_F64, "star7"), (BK_F32, "cube27"),
+                                        (BK_F32, "star7"), (BK_BF16, "star13")])
+def test_output_field_off_the_pair_boundary(dtype, name):
+    """An output field whose bricks start at odd element offsets (step 2 x 512 + 1, offset 1)
+    takes kernels that store one element at a time; the results match the oracle."""
+    st = stencils.make(name, 3)
+    dom = GridDomain(32, dtype=dtype)
+    arr = stencils.uniform(19, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    ost = B.BrickStorage.allocate_device(dom.nbricks, 2 * dom.bsize + 1, dtype)
+    bout = B.Brick(dom.dev_info, ost, 1, dom.layout)
+    assert B.sweepKernel(dom.brick(0), bout, st) in ("sweep_kernel", "sweep_star_tma_kernel")
+    B.brickSweep(dom.brick(0), bout, dom.dev_interior, st)
+    B.synchronize()
+    assert B.error_flags() == 0
+    host = B.movBrickStorage(ost, to_device=False).host.reshape(dom.nbricks, -1)
+    dom.storage.host.reshape(dom.nbricks, dom.nfields, -1)[:, 1, :] = host[:, 1:1 + dom.bsize]
+    got = dom.interior_view(dom.get_field(1))
+    if dtype == BK_F64:
+        ok, md = mixed_ok(got, oracle_array(dom, arr, st))
+        assert ok, f"max |diff| {md}"
+    elif dtype == BK_F32:
+        assert normwise(got, oracle_array(dom, arr.astype(np.float32).astype(np.float64), st)) <= 1e-5
+    else:
+        arr_b = B.bf16_to_f32(B.f32_to_bf16(arr.astype(np.float32))).astype(np.float64)
+        assert normwise(got, oracle_array(dom, arr_b, st)) <= 2.0 ** -7
 
 
 @pytest.mark.parametrize("name,acc", [("star7", BK_ACC_NATIVE), ("cube27", BK_ACC_NATIVE),

@@ -52,12 +52,15 @@ def test_stencil_families():
     assert f == 0
 
 
-def _kernel_for(name, lay=None, dtype=_abi.BK_F64, acc=_abi.BK_ACC_NATIVE, offset=0, base=1 << 20):
-    """bk_sweep_kernel on host-only field descriptors (the pointer is never dereferenced)."""
+def _kernel_for(name, lay=None, dtype=_abi.BK_F64, acc=_abi.BK_ACC_NATIVE, offset=0, base=1 << 20, odd_out=False):
+    """bk_sweep_kernel on host-only field descriptors (the pointer is never dereferenced);
+    `odd_out`: an output storage of step 2 x size + 1 with the field at offset 1."""
     lay = lay or B.Layout()
     size = lay.size
     fin = _abi.bk_field(C.c_void_p(base), 100, 2 * size, offset, dtype)
     fout = _abi.bk_field(C.c_void_p(base), 100, 2 * size, size if offset == 0 else 0, dtype)
+    if odd_out:
+        fout = _abi.bk_field(C.c_void_p(base + (1 << 24)), 100, 2 * size + 1, 1, dtype)
     out = C.c_char_p()
     _abi.call("bk_sweep_kernel", C.byref(fin), C.byref(fout), C.byref(B.to_c_stencil(stencils.make(name, 1))),
               C.byref(lay.to_c()), acc, C.byref(out))
@@ -86,6 +89,11 @@ def test_kernel_choice(monkeypatch):
     assert _kernel_for("star7", lay=B.Layout((8, 8, 8), (1, 2, 2))) == "sweep_kernel"
     assert _kernel_for("star7", lay=B.Layout((4, 4, 4), (1, 4, 4))) == "sweep2_kernel"
     assert _kernel_for("star7", base=(1 << 20) + 8) == "sweep_kernel"  # not 16-byte aligned
+    # output bricks off the two-element boundary: no kernel that stores output pairs
+    assert _kernel_for("cube125", odd_out=True) == "sweep_kernel"
+    assert _kernel_for("cube27", dtype=_abi.BK_F32, odd_out=True) == "sweep_kernel"
+    assert _kernel_for("star7", dtype=_abi.BK_F32, odd_out=True) == "sweep_star_tma_kernel"
+    assert _kernel_for("star7", odd_out=True) == "sweep_star_tma_kernel"
     monkeypatch.setenv("BK_SWEEP_PIPELINED", "1")
     assert _kernel_for("star7") == "sweep2_kernel"
     monkeypatch.setenv("BK_SWEEP_ONESHOT", "1")
