@@ -255,11 +255,11 @@ def run_ours(args):
 
     # end to end through the public API, every result in host memory.  Per step: the input is
     # copied from page-locked memory (on a copy stream, into one of two device buffers, while the
-    # previous step sweeps); each sweep but the last writes its own device buffer, whose
-    # device-to-host copy runs on a second copy stream under the following sweeps (one buffer per
-    # stencil, so no sweep waits for an earlier result to leave its buffer); the last sweep
-    # stores its result straight into mapped page-locked host memory (bk_host_malloc) over
-    # NVLink-C2C.  The link carries the input and the results in opposite directions.
+    # previous step sweeps); each sweep writes its own device buffer, whose device-to-host copy runs
+    # on a second copy stream under the following sweeps (one buffer per stencil, so no sweep waits
+    # for an earlier result to leave its buffer, and the last results of a step leave under the
+    # next step's first sweeps).  The link carries the input and the results in opposite
+    # directions; the results (five fields per step) keep the device-to-host direction busy.
     e2e = None
     if not args.no_e2e:
         nbytes = nbricks * bsize * esize
@@ -267,7 +267,7 @@ def run_ours(args):
         s_in2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
         ins = [B.Brick(dinfo, s_in, 0, lay), B.Brick(dinfo, s_in2, 0, lay)]
         s_out2 = B.BrickStorage.allocate_device(nbricks, bsize, dtype)
-        nbuf = max(2, len(shapes) - 1)
+        nbuf = max(2, len(shapes))
         s_outs = [s_out, s_out2] + [B.BrickStorage.allocate_device(nbricks, bsize, dtype) for _ in range(nbuf - 2)]
         outs = [B.Brick(dinfo, so, 0, lay) for so in s_outs]
         h_outs = {}
@@ -281,7 +281,7 @@ def run_ours(args):
         consumed = [torch.cuda.Event(), torch.cuda.Event()]
         swept = [torch.cuda.Event() for _ in range(nbuf)]
         copied = [torch.cuda.Event() for _ in range(nbuf)]
-        Ke = max(1, min(K, 5))
+        Ke = max(1, min(K, 10))
 
         def h2d(buf):
             cin.wait_event(consumed[buf])
@@ -303,9 +303,6 @@ def run_ours(args):
                 h2d(1 - cur)  # the next step's input, while this step sweeps
             stream.wait_event(arrived[cur])
             for q, name in enumerate(shapes):
-                if q == len(shapes) - 1:
-                    B.brickSweep(ins[cur], B.Brick(dinfo, h_outs[name], 0, lay), blist, csts[name], acc, stream=sp)
-                    continue
                 ob = q % nbuf
                 stream.wait_event(copied[ob])  # its previous result has left the buffer
                 B.brickSweep(ins[cur], outs[ob], blist, csts[name], acc, stream=sp)
@@ -341,10 +338,10 @@ def run_ours(args):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3),
                "link_alone": link,
                "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a copy "
-                       "stream under the previous step's sweeps; results: device-to-host copies on a second "
-                       "stream under the following sweeps (one device buffer per stencil), the last sweep "
-                       "storing straight into mapped page-locked host memory over NVLink-C2C; one host buffer "
-                       "per stencil"}
+                       "stream under the previous step's sweeps; results: device-to-host copies into page-locked "
+                       "memory on a second stream under the following sweeps (one device buffer per stencil, the "
+                       "last results of a step leaving under the next step's first sweeps); one host buffer per "
+                       "stencil"}
 
     # the other FP64 arithmetic mode on the same data: per-stencil rate and its normwise
     # error against the first mode's output
