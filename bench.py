@@ -288,34 +288,40 @@ def run_ours(args):
             B.memcpy(ins[buf].bStorage.ptr, h_in.ptr, nbytes, 0, cin.cuda_stream)
             arrived[buf].record(cin)
 
-        for q in range(2):
-            consumed[q].record(stream)
-        for q in range(nbuf):
-            copied[q].record(stream)
-        h2d(0)
-        for it in range(Ke + 1):
-            cur = it % 2
-            if it == 1:
-                torch.cuda.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            if it < Ke:
-                h2d(1 - cur)  # the next step's input, while this step sweeps
-            stream.wait_event(arrived[cur])
-            for q, name in enumerate(shapes):
-                ob = q % nbuf
-                stream.wait_event(copied[ob])  # its previous result has left the buffer
-                B.brickSweep(ins[cur], outs[ob], blist, csts[name], acc, stream=sp)
-                swept[ob].record(stream)
-                cout.wait_event(swept[ob])
-                B.memcpy(h_outs[name].ptr, outs[ob].bStorage.ptr, nbytes, 1, cout.cuda_stream)
-                copied[ob].record(cout)
-            consumed[cur].record(stream)
-        for q in range(nbuf):
-            stream.wait_event(copied[q])
-        e1.record(stream)
-        torch.cuda.synchronize()
-        e_ms = max_over_ranks(e0.elapsed_time(e1) / Ke)
+        def e2e_trial():
+            """Ke timed steps after one untimed step; ms per step."""
+            for q in range(2):
+                consumed[q].record(stream)
+            for q in range(nbuf):
+                copied[q].record(stream)
+            h2d(0)
+            for it in range(Ke + 1):
+                cur = it % 2
+                if it == 1:
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                if it < Ke:
+                    h2d(1 - cur)  # the next step's input, while this step sweeps
+                stream.wait_event(arrived[cur])
+                for q, name in enumerate(shapes):
+                    ob = q % nbuf
+                    stream.wait_event(copied[ob])  # its previous result has left the buffer
+                    B.brickSweep(ins[cur], outs[ob], blist, csts[name], acc, stream=sp)
+                    swept[ob].record(stream)
+                    cout.wait_event(swept[ob])
+                    B.memcpy(h_outs[name].ptr, outs[ob].bStorage.ptr, nbytes, 1, cout.cuda_stream)
+                    copied[ob].record(cout)
+                consumed[cur].record(stream)
+            for q in range(nbuf):
+                stream.wait_event(copied[q])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return max_over_ranks(e0.elapsed_time(e1) / Ke)
+
+        # three trials, the median reported: the host link is shared with other work on the node
+        trials = [e2e_trial() for _ in range(3)]
+        e_ms = statistics.median(trials)
         # the link rates this box gives alone (after the timed region): one copy each way
         link = {}
         for key, dst, src, kind in (("h2d_gbs", s_in2.ptr, h_in.ptr, 0),
@@ -336,6 +342,7 @@ def run_ours(args):
                 raise RuntimeError(f"{name}: the result in host memory differs from the device sweep")
         e2e = {"value": round(ws * len(shapes) * points / (e_ms * 1e-3) / 1e9, 3), "unit": "GStencil/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes * len(shapes), "ms_per_step": round(e_ms, 3),
+               "trials_ms_per_step": [round(x, 3) for x in trials],
                "link_alone": link,
                "path": "input: cudaMemcpyAsync from page-locked memory into one of two device buffers on a copy "
                        "stream under the previous step's sweeps; results: device-to-host copies into page-locked "

@@ -1,9 +1,12 @@
 // Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
-// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 256 threads: a
-// brick's (4+2R)^4 neighbourhood is gathered into shared memory by asynchronous copies (the
-// source slot and in-brick offset of every tile element from a table the CTA builds once)
-// while the previous brick is computed, one element per thread.  Out-of-range list or adjacency entries are clamped / skipped and
-// raise the device error flag, as in the 3-D kernels.
+// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 256 threads: the
+// part of a brick's neighbourhood the stencil reads (centre and faces for a star, the whole
+// radius-R box otherwise) is gathered into shared memory by asynchronous copies while the
+// previous brick is computed, one output per thread.  The copies follow a table the CTA builds
+// once from the layout: one entry per 16-byte block of a tile row, a single 16-byte copy where
+// the block's elements are consecutive in their brick, else one copy per element.  Out-of-range
+// list or adjacency entries are clamped / skipped and raise the device error flag, as in the
+// 3-D kernels.
 #include "bk_common.cuh"
 
 namespace bk {
@@ -22,58 +25,99 @@ struct Layout4 {
 
 struct Taps4 {
   int n;
-  int toff[BK_MAX_TAPS4];  // offsets in the (4+2R)^4 tile
+  int toff[BK_MAX_TAPS4];  // offsets in the E x E x E x EI tile (Tile4)
   double c[BK_MAX_TAPS4];
   float cf[BK_MAX_TAPS4];
 };
 
-// Element copy global -> shared through the asynchronous copy path (4 or 8 bytes).
+// Element copy global -> shared through the asynchronous copy path (4, 8 or 16 bytes).
 template <int BYTES>
 __device__ __forceinline__ void cp_async_elem(unsigned dst, const void *src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit4() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait4() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Tile of one brick's neighbourhood: E = 4 + 2R along l, k, j; along i the halo is rounded up
+// to whole 16-byte blocks (RP elements a side), EI = 4 + 2 RP, so that each block of a row lies
+// in one brick and the centre blocks start 16-byte aligned.
+template <typename T, int R>
+struct Tile4 {
+  static constexpr int ES = (int)sizeof(T), VE = 16 / ES, RP = (R + VE - 1) / VE * VE;
+  static constexpr int E = 4 + 2 * R, EI = 4 + 2 * RP, ROWS = E * E * E, NBLK = EI / VE;
+  static constexpr int NENT = ROWS * NBLK, TILE = ROWS * EI;
+  static constexpr size_t SMEM = 2 * (size_t)TILE * ES + (size_t)NENT * 8;
+};
+
 // Persistent CTAs walk the brick list with a stride of the grid, pipelined: while brick j is
 // computed from one tile buffer, brick j+1's neighbourhood is gathered into the other by
 // asynchronous copies, and brick j+2's list and adjacency entries are staged (three
 // adjacency slots, so no slot is rewritten while read).  Two block barriers per brick.
+// star: every tap has at most one non-zero offset (only centre and face elements are read);
+// vec: the input field's bricks start 16-byte aligned (16-byte copies allowed).
 template <typename T, typename AT, int R>
 __global__ void __launch_bounds__(256)
 sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__restrict__ in, unsigned long long in_step,
               long long in_chunks, T *__restrict__ out, unsigned long long out_step, long long out_chunks,
-              const unsigned *__restrict__ blist, unsigned nlist, const Layout4 L, const Taps4 tp, int *err) {
+              const unsigned *__restrict__ blist, unsigned nlist, const Layout4 L, const Taps4 tp, int star, int vec,
+              int *err) {
   static_assert(sizeof(T) == sizeof(AT) && (sizeof(T) == 4 || sizeof(T) == 8), "the tile holds the storage type");
-  constexpr int B = 4, E = B + 2 * R, TILE = E * E * E * E;
+  typedef Tile4<T, R> G;
+  constexpr int B = 4, E = G::E, EI = G::EI, VE = G::VE, RP = G::RP, NBLK = G::NBLK, NENT = G::NENT, TILE = G::TILE;
+  static_assert(TILE < (1 << 14), "tile offsets take 14 bits");
   constexpr unsigned NONE = 0xFFFFFFFFu;
-  // dynamic shared memory: tile[2][TILE], then where every tile element comes from (offset in
-  // its brick, adjacency slot): fixed by the layout, so computed once per CTA
+  // dynamic shared memory: tile[2][TILE], then the copy table: per (row, block) entry a word
+  // slot (7 bits) | tile offset (14) << 7 | element mask (VE bits) << 21 | kind << 30
+  // (0 nothing, 1 one 16-byte copy, 2 one copy per element of the mask) and a word of the
+  // elements' in-brick offsets (8 bits each)
   extern __shared__ __align__(16) unsigned char smem4[];
   T(*tile)[TILE] = reinterpret_cast<T(*)[TILE]>(smem4);
-  unsigned short *toffs = reinterpret_cast<unsigned short *>(smem4 + 2 * TILE * sizeof(T));
-  unsigned char *tslot = reinterpret_cast<unsigned char *>(toffs + TILE);
+  unsigned *plan = reinterpret_cast<unsigned *>(smem4 + 2 * TILE * sizeof(T));
+  unsigned *srcw = plan + NENT;
   __shared__ unsigned nbr[3][81];
   const int t = threadIdx.x;
-  for (int e = t; e < TILE; e += blockDim.x) {
-    int r = e;
-    const int ii = r % E; r /= E;
-    const int jj = r % E; r /= E;
-    const int kk = r % E;
-    const int ll = r / E;
-    const int ql = ll < R ? -1 : (ll >= R + B ? 1 : 0), qk = kk < R ? -1 : (kk >= R + B ? 1 : 0);
-    const int qj = jj < R ? -1 : (jj >= R + B ? 1 : 0), qi = ii < R ? -1 : (ii >= R + B ? 1 : 0);
-    tslot[e] = (unsigned char)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
-    toffs[e] = (unsigned short)L.offset(ll - R - ql * B, kk - R - qk * B, jj - R - qj * B, ii - R - qi * B);
+  for (int e = t; e < NENT; e += blockDim.x) {
+    const int row = e / NBLK, blk = e - row * NBLK;
+    const int l = row / (E * E) - R, k = (row / E) % E - R, j = row % E - R;  // in-brick, may lie outside
+    const int ql = l < 0 ? -1 : (l >= B ? 1 : 0), qk = k < 0 ? -1 : (k >= B ? 1 : 0);
+    const int qj = j < 0 ? -1 : (j >= B ? 1 : 0);
+    const int i0 = blk * VE - RP;  // the block's first i
+    const int qi = i0 < 0 ? -1 : (i0 >= B ? 1 : 0);
+    const int outside = (ql != 0) + (qk != 0) + (qj != 0) + (qi != 0);
+    unsigned mask = 0, sw = 0;
+    bool consecutive = true;
+    int s0 = -1;
+    for (int q = 0; q < VE; ++q) {
+      const int i = i0 + q;
+      if (i < -R || i >= B + R || (star && outside > 1)) continue;
+      const int so = L.offset(l - ql * B, k - qk * B, j - qj * B, i - qi * B);
+      if (q == 0) s0 = so;
+      if (so != s0 + q) consecutive = false;
+      mask |= 1u << q;
+      sw |= (unsigned)so << (8 * q);
+    }
+    unsigned w = 0;
+    if (mask) {
+      const unsigned slot = (unsigned)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
+      const bool v16 = vec && consecutive && mask == (1u << VE) - 1u && s0 % VE == 0;
+      w = slot | ((unsigned)(row * EI + blk * VE) << 7) | (mask << 21) | ((v16 ? 1u : 2u) << 30);
+    }
+    plan[e] = w;
+    srcw[e] = sw;
   }
   const unsigned long long gs = gridDim.x;
-  // this thread's adjacency entry (slot t < 81) of list entry n; slot 40 carries NONE for a
-  // brick that is not computed (past the list, or out of range: flagged)
-  auto fetch = [&](unsigned long long n) -> unsigned {
-    if (t >= 81) return 0u;
+  // Staging of list entry n's adjacency row (thread t < 81 holds slot t): the list entry is
+  // loaded two iterations and the adjacency row one iteration before the row is staged, so no
+  // iteration waits for a load it issued.  check() gives the staged value: slot 40 carries
+  // NONE for a brick that is not computed (past the list, or out of range: flagged).
+  auto load_b = [&](unsigned long long n) -> unsigned { return (t < 81 && n < nlist) ? blist[n] : NONE; };
+  auto load_v = [&](unsigned b) -> unsigned { return (t < 81 && b < nbricks) ? adj[(size_t)b * 81 + t] : 0u; };
+  auto check = [&](unsigned long long n, unsigned b, unsigned v) -> unsigned {
     if (n >= nlist) return t == 40 ? NONE : 0u;
-    const unsigned b = blist[n];
     if (b >= nbricks) {
       if (t == 40) {
         atomicOr(err, FLAG_BOUNDS);
@@ -81,10 +125,9 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
       }
       return 0u;
     }
-    unsigned v = adj[(size_t)b * 81 + t];
     if ((long long)v >= in_chunks || (t == 40 && (long long)v >= out_chunks)) {
       atomicOr(err, FLAG_BOUNDS);
-      v = t == 40 ? NONE : 0u;
+      return t == 40 ? NONE : 0u;
     }
     return v;
   };
@@ -92,35 +135,57 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     const unsigned *nb = nbr[slot];
     if (nb[40] != NONE) {
       const unsigned base = (unsigned)__cvta_generic_to_shared(&tile[buf][0]);
-      for (int e = t; e < TILE; e += blockDim.x)
-        cp_async_elem<sizeof(T)>(base + e * (unsigned)sizeof(T), in + (size_t)nb[tslot[e]] * in_step + toffs[e]);
+      for (int e = t; e < NENT; e += blockDim.x) {
+        const unsigned w = plan[e];
+        if (!w) continue;
+        const T *src = in + (size_t)nb[w & 127u] * in_step;
+        const unsigned dst = base + ((w >> 7) & 0x3FFFu) * (unsigned)sizeof(T);
+        const unsigned sw = srcw[e];
+        if ((w >> 30) == 1u) {
+          cp_async_elem<16>(dst, src + (sw & 255u));
+        } else {
+#pragma unroll
+          for (int q = 0; q < VE; ++q)
+            if ((w >> (21 + q)) & 1u) cp_async_elem<sizeof(T)>(dst + q * (unsigned)sizeof(T), src + ((sw >> (8 * q)) & 255u));
+        }
+      }
     }
     cp_async_commit4();
   };
   const unsigned long long n0 = blockIdx.x;
   {
-    const unsigned a0 = fetch(n0), a1 = fetch(n0 + gs);
+    const unsigned b0 = load_b(n0), b1 = load_b(n0 + gs);
+    const unsigned a0 = check(n0, b0, load_v(b0)), a1 = check(n0 + gs, b1, load_v(b1));
     if (t < 81) {
       nbr[0][t] = a0;
       nbr[1][t] = a1;
     }
   }
-  unsigned ahead = fetch(n0 + 2 * gs);
+  unsigned ba = load_b(n0 + 2 * gs);  // list entry n + 2 gs and its adjacency row
+  unsigned va = load_v(ba);
+  unsigned bb = load_b(n0 + 3 * gs);  // list entry n + 3 gs
   __syncthreads();  // tables and the first two adjacency slots
   issue(0, 0);
-  int j = 0;
-  for (unsigned long long n = n0; n < nlist; n += gs, ++j) {
-    const int cur = j % 3, nxt = (j + 1) % 3, far = (j + 2) % 3, buf = j & 1;
+  // this thread's output element: its tile position and its in-brick offset (the layout's
+  // divisions by the fold, once per kernel instead of once per brick)
+  const int oi = t % B, oj = (t / B) % B, ok = (t / (B * B)) % B, ol = t / (B * B * B);
+  const int ctile = (((ol + R) * E + (ok + R)) * E + (oj + R)) * EI + (oi + RP);
+  const int oofs = t < B * B * B * B ? L.offset(ol, ok, oj, oi) : 0;
+  int jb = 0;
+  for (unsigned long long n = n0; n < nlist; n += gs, ++jb) {
+    const int cur = jb % 3, nxt = (jb + 1) % 3, far = (jb + 2) % 3, buf = jb & 1;
     __syncthreads();  // the previous brick's compute is done with tile[buf ^ 1] and slot far
     issue(nxt, buf ^ 1);
-    if (t < 81) nbr[far][t] = ahead;
-    ahead = fetch(n + 3 * gs);
+    const unsigned staged = check(n + 2 * gs, ba, va);
+    if (t < 81) nbr[far][t] = staged;
+    ba = bb;
+    va = load_v(bb);
+    bb = load_b(n + 4 * gs);
     cp_async_wait4<1>();  // this thread's copies for brick n have landed
     __syncthreads();      // ... and everybody else's
     const unsigned ob = nbr[cur][40];
     if (ob != NONE && t < B * B * B * B) {
-      const int i = t % B, jj = (t / B) % B, k = (t / (B * B)) % B, l = t / (B * B * B);
-      const T *c = tile[buf] + (((l + R) * E + (k + R)) * E + (jj + R)) * E + (i + R);
+      const T *c = tile[buf] + ctile;
       AT v;
       if constexpr (sizeof(AT) == 8) {
         v = tp.c[0] * c[tp.toff[0]];
@@ -129,7 +194,7 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
         v = tp.cf[0] * c[tp.toff[0]];
         for (int q = 1; q < tp.n; ++q) v = fmaf(tp.cf[q], c[tp.toff[q]], v);
       }
-      Elem<T>::store(out + (size_t)ob * out_step + L.offset(l, k, jj, i), v);
+      Elem<T>::store(out + (size_t)ob * out_step + oofs, v);
     }
   }
   cp_async_wait4<0>();  // no copy may outlive the kernel
@@ -137,11 +202,17 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
 
 template <typename T, typename AT, int R>
 static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
-                   unsigned nlist, const Layout4 &L, const Taps4 &tp, int *err, cudaStream_t s) {
-  // persistent CTAs (each builds its tile table once): as many as fit on the GPU
+                   unsigned nlist, const Layout4 &L, Taps4 tp, const int (*offs)[4], int star, cudaStream_t s) {
+  // persistent CTAs (each builds its copy table once): as many as fit on the GPU
+  typedef Tile4<T, R> G;
   auto kern = sweep4_kernel<T, AT, R>;
-  constexpr int E = 4 + 2 * R, TILE = E * E * E * E;
-  constexpr size_t smem = 2 * TILE * sizeof(T) + TILE * 3;
+  constexpr size_t smem = G::SMEM;
+  for (int t = 0; t < tp.n; ++t)
+    tp.toff[t] = ((offs[t][0] * G::E + offs[t][1]) * G::E + offs[t][2]) * G::EI + offs[t][3];
+  const char *ibase = reinterpret_cast<const char *>(in->dat) + in->offset * sizeof(T);
+  const int vec = reinterpret_cast<uintptr_t>(ibase) % 16 == 0 && (in->step * sizeof(T)) % 16 == 0;
+  int *err = device_error_word();
+  if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e0 = cudaGetDevice(&dev);
   if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -153,7 +224,7 @@ static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, co
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, 256, smem, s>>>(
       adj, nbricks, reinterpret_cast<const T *>(in->dat) + in->offset, in->step, in->chunks,
-      reinterpret_cast<T *>(out->dat) + out->offset, out->step, out->chunks, blist, nlist, L, tp, err);
+      reinterpret_cast<T *>(out->dat) + out->offset, out->step, out->chunks, blist, nlist, L, tp, star, vec, err);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "sweep4 launch");
   return BK_OK;
@@ -192,23 +263,22 @@ int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const b
   if (r > 2) return fail(BK_ERR_UNSUPPORTED, "4-D stencils of radius up to 2");
   if (nlist == 0) return BK_OK;
   if (!adj || !blist || nbricks == 0) return fail(BK_ERR_ARG, "adjacency, brick list and nbricks are required");
-  const int R = r <= 1 ? 1 : 2, E = 4 + 2 * R;
+  const int R = r <= 1 ? 1 : 2;
   Taps4 tp;
   tp.n = st->npoints;
+  int star = 1;
   for (int t = 0; t < tp.n; ++t) {
     const int *o = st->offsets[t];
-    tp.toff[t] = ((o[0] * E + o[1]) * E + o[2]) * E + o[3];
+    star = star && ((o[0] != 0) + (o[1] != 0) + (o[2] != 0) + (o[3] != 0) <= 1);
     tp.c[t] = st->coeff[t];
     tp.cf[t] = (float)st->coeff[t];
   }
-  int *err = device_error_word();
-  if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
   cudaStream_t s = as_stream(stream);
   if (in->dtype == BK_F64)
-    return R == 1 ? launch4<double, double, 1>(adj, nbricks, in, out, blist, nlist, L, tp, err, s)
-                  : launch4<double, double, 2>(adj, nbricks, in, out, blist, nlist, L, tp, err, s);
-  return R == 1 ? launch4<float, float, 1>(adj, nbricks, in, out, blist, nlist, L, tp, err, s)
-                : launch4<float, float, 2>(adj, nbricks, in, out, blist, nlist, L, tp, err, s);
+    return R == 1 ? launch4<double, double, 1>(adj, nbricks, in, out, blist, nlist, L, tp, st->offsets, star, s)
+                  : launch4<double, double, 2>(adj, nbricks, in, out, blist, nlist, L, tp, st->offsets, star, s);
+  return R == 1 ? launch4<float, float, 1>(adj, nbricks, in, out, blist, nlist, L, tp, st->offsets, star, s)
+                : launch4<float, float, 2>(adj, nbricks, in, out, blist, nlist, L, tp, st->offsets, star, s);
 }
 
 }  // extern "C"

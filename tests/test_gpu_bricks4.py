@@ -124,3 +124,37 @@ def test_sweep4_periodic_steps_over_brickdecomp():
     sl = (slice(o, o + n),) * 4
     ok, md = mixed_ok(out[sl], a[sl])
     assert ok, f"max |diff| {md}"
+
+
+@pytest.mark.parametrize("dtype", [_abi.BK_F64, _abi.BK_F32])
+@pytest.mark.parametrize("fold", [(1, 1, 2, 4), (1, 1, 2, 2)])
+def test_sweep4_element_copies_equal_vector_copies(dtype, fold):
+    """Input bricks off the 16-byte boundary (storage step 513) take one copy per element
+    instead of 16-byte copies of whole row blocks: the same bits as the aligned storage, for a
+    star (centre and faces fetched) and a radius-2 box (every element within the radius)."""
+    gb = 6  # 4^4 interior bricks with one ghost brick a side
+    grid, adj = B4.init_grid([gb] * 4)
+    nb = len(grid)
+    np_dt = B.NP_DTYPE[dtype]
+    data = stencils.uniform(21, nb * 256).astype(np_dt).reshape(nb, 256)
+    adj_dev = B.DeviceBuffer(adj.nbytes)
+    adj_dev.upload(adj)
+    g4 = grid.reshape((gb,) * 4)
+    inner = B.BrickList(np.ascontiguousarray(g4[1:-1, 1:-1, 1:-1, 1:-1].reshape(-1)))
+    lay = B4.Layout4(fold=fold)
+    box = [tuple(int(a) - 2 for a in t) for t in np.ndindex(5, 5, 5, 5)]
+    pick = np.random.default_rng(4).choice(len(box), size=81, replace=False)
+    sts = [B4.mpi9pt(), stencils.Stencil("box81", [box[q] for q in pick], stencils.uniform01(4, 81))]
+    for st in sts:
+        outs = []
+        for step in (512, 513):
+            store = np.zeros((nb, step), np_dt)
+            store[:, :256] = data
+            sdev = B.BrickStorage(nb, step, dtype, device=B.DeviceBuffer(store.nbytes))
+            sdev.device.upload(store)
+            B4.sweep4(adj_dev, nb, sdev, 0, step - 256, inner, st, lay)
+            B.synchronize()
+            assert B.error_flags() == 0
+            sdev.device.download(store)
+            outs.append(store[:, step - 256:].copy())
+        np.testing.assert_array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8), err_msg=st.name)
