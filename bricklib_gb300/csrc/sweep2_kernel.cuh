@@ -1,6 +1,8 @@
 // Pipelined brick sweep for row-major brick layouts (sweep_kernel covers the rest).
 //
-// Persistent CTAs walk the brick list in groups of NB bricks.  For every group:
+// Persistent CTAs walk the brick list in groups of NB bricks (every gridDim.x-th group; a
+// contiguous share of the list per CTA for the FP64 mirror-symmetric cubes streamed along i,
+// sym_cube_istream).  For every group:
 //   * the 27 adjacency entries of each brick are staged in shared memory;
 //   * every thread issues its share of the group's gather as asynchronous global->shared
 //     copies (cp.async, 16 bytes where the layout allows) into one of two tile buffers,
@@ -12,8 +14,9 @@
 //     buffer.
 // Compute: each thread owns one (j, i) column of a brick; the column's k-extended values
 // sit in registers, so k-direction taps cost no shared-memory loads; star stencils read
-// the i / j taps from the tile, cube stencils walk the (2R+1)^2 columns.  Float-float mode
-// converts the raw FP64 tile into float pairs in one pass before computing.
+// the i / j taps from the tile, cube stencils walk the (2R+1)^2 columns (the 8x8x8 cube
+// paths: a column pair per lane, or, streamed along i, two rows per lane).  Float-float
+// mode converts the raw FP64 tile into float pairs in one pass before computing.
 #pragma once
 
 #include "sweep_kernel.cuh"

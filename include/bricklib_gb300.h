@@ -157,11 +157,16 @@ int bk_stencil_check(const bk_stencil *st, const bk_layout *lay, int *radius, in
  * Four kernels implement it: two TMA-fed ones for 7/13/25-point stars on row-major 8x8x8
  * bricks with 16-byte aligned input (FP32 / BF16: runs of i-adjacent list entries share
  * their i-neighbour bricks; FP64: per-brick staging), a pipelined one (row-major layouts,
- * 16-byte aligned input) and a one-shot one (everything).  The environment variables
+ * 16-byte aligned input; FP64 mirror-symmetric cubes carry per-column sums along runs of
+ * i-adjacent list entries, so a list in grid order is fastest) and a one-shot one
+ * (everything).  The FP32 / BF16 row kernel and the cube kernels on 8x8x8 bricks store
+ * output pairs: they need every output brick to start on a two-element boundary, and
+ * other output fields take per-element stores.  The environment variables
  * BK_SWEEP_ONESHOT=1 and BK_SWEEP_PIPELINED=1 override the built-in choice (used by the
  * parity tests); BK_TMA_ROW=0 selects per-brick staging for FP32 / BF16, BK_TMA_GROUP=0/1
  * turns the row kernel's grouped copies of full runs off/on, BK_TMA_STAGES (2..4) and
- * BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernels. */
+ * BK_TMA_IFACE (narrow / whole) tune the TMA-fed kernels, BK_SWEEP_ISTREAM=0 computes
+ * FP64 mirror-symmetric cubes one brick at a time. */
 int bk_sweep(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out,
              const unsigned *blist, unsigned nlist, const bk_stencil *st, const bk_layout *lay,
              int acc, void *stream);
