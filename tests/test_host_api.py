@@ -199,3 +199,22 @@ def test_periodic_adjacency_points_at_wrapped_interior_bricks(nb):
                     assert wadj[b, s] == g3[wk, wj, wi], (b, s)
                     if 1 <= k + dk <= nb[0] and 1 <= j + dj <= nb[1] and 1 <= i + di <= nb[2]:
                         assert wadj[b, s] == info.adj[b, s]
+
+
+def test_bench_instruction_counts_follow_the_symmetry_the_kernels_use():
+    """bench.py's floating-point instructions per point (the numerator of roofline.compute
+    pipe_frac) follow the coefficient symmetry the kernels exploit: FP64 mirror-symmetric cubes
+    stream along i (37 with k <-> j symmetry, 43 without), FP32 ones sum classes on column pairs,
+    a cube without the symmetry takes a multiply-add per tap."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    from tests.test_gpu_sweep import _mirror_symmetric_cube
+    nat = _abi.BK_ACC_NATIVE
+    assert bench.fp_instructions_per_point(stencils.make("cube125", 3), nat, _abi.BK_F64) == 37.0
+    assert bench.fp_instructions_per_point(_mirror_symmetric_cube(2, 5), nat, _abi.BK_F64) == 43.0
+    assert bench.fp_instructions_per_point(_mirror_symmetric_cube(1, 5, kj=True), nat, _abi.BK_F64) == 13.0
+    assert bench.fp_instructions_per_point(_mirror_symmetric_cube(2, 5, ij=True), nat, _abi.BK_F32) == 58.5
+    assert bench.fp_instructions_per_point(stencils.make("cube27", 3), nat, _abi.BK_F64) == 27.0
+    assert bench.fp_instructions_per_point(stencils.make("star25", 3), nat, _abi.BK_F64) == 25.0
+    assert bench.fp_instructions_per_point(stencils.make("cube125", 3), _abi.BK_ACC_FLOATFLOAT, _abi.BK_F64) == 125.0
