@@ -416,7 +416,7 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
   constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP, NW = 2 * R + 1;
   static_assert(R == 1 || R == 2, "cube radius");
   const int k0 = 2 * (lane >> 3), j = lane & 7;
-  double *col = rt + (k0 + R) * SK + (j + R) * SJ;  // tile (brick k0, brick j, column 0)
+  double *col = rt + (k0 + R) * SK + (j + R) * SJ;  // tile row of brick-local (k0, j), column 0
   // W_a of tile column ii for both rows, pushed into the window (newest at NW - 1)
   auto column = [&](const int ii) {
     double H[R + 1][2 * R + 2];  // H[b][q]: plane k0 - R + q
