@@ -159,6 +159,17 @@ def error_flags(stream=None) -> int:
     return f.value
 
 
+def check_device(stream=None) -> None:
+    """Reads and clears the device error flags; raises BkError with BK_ERR_TIMEOUT when a
+    bounded device wait gave up (the launch stopped early and its output is incomplete) and
+    with BK_ERR_BOUNDS when an out-of-range brick index was clamped or skipped."""
+    f = error_flags(stream)
+    if f & 2:
+        raise _abi.BkError(_abi.BK_ERR_TIMEOUT, "a bounded device wait gave up; the launch stopped early")
+    if f & 1:
+        raise _abi.BkError(_abi.BK_ERR_BOUNDS, "an out-of-range brick index was clamped or skipped")
+
+
 # ------------------------------------------------------------------ layout
 
 @dataclass(frozen=True)

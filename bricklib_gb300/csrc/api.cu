@@ -66,6 +66,27 @@ int check_field(const bk_field *f, const Layout &L, const char *name) {
   return BK_OK;
 }
 
+// A sweep reads `in` and writes `out`, so no output element may be an input element.  Fields
+// in separate storages are disjoint; fields of one storage (same base and step, the
+// interleaved bIn / bOut of stencils/3axis.cpp:26-28) are disjoint when their offsets are a
+// brick apart.  Anything else whose byte ranges meet (one storage seen with two steps, or two
+// storages that overlap in memory) is rejected.
+int check_disjoint(const bk_field *in, const bk_field *out, size_t brick_elems) {
+  const size_t es_in = dtype_size(in->dtype), es_out = dtype_size(out->dtype);
+  if (in->dat == out->dat && in->step == out->step && es_in == es_out) {
+    const size_t lo = in->offset < out->offset ? in->offset : out->offset;
+    const size_t hi = in->offset < out->offset ? out->offset : in->offset;
+    if (hi - lo < brick_elems) return fail(BK_ERR_ARG, "in and out fields overlap");
+    return BK_OK;
+  }
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(in->dat), b0 = reinterpret_cast<uintptr_t>(out->dat);
+  const uintptr_t a1 = a0 + (uintptr_t)in->chunks * in->step * es_in;
+  const uintptr_t b1 = b0 + (uintptr_t)out->chunks * out->step * es_out;
+  if (a0 < b1 && b0 < a1)
+    return fail(BK_ERR_ARG, "in and out fields share storage bytes with a different base or step");
+  return BK_OK;
+}
+
 }  // namespace bk
 
 using namespace bk;

@@ -76,5 +76,6 @@ struct Layout {
 
 int check_layout(const bk_layout *lay, Layout *out);
 int check_field(const bk_field *f, const Layout &L, const char *name);
+int check_disjoint(const bk_field *in, const bk_field *out, size_t brick_elems);
 
 }  // namespace bk

@@ -145,11 +145,7 @@ static int plan_sweep(const bk_field *in, const bk_field *out, const bk_stencil 
   if ((s = check_field(in, L, "in"))) return s;
   if ((s = check_field(out, L, "out"))) return s;
   if (in->dtype != out->dtype) return fail(BK_ERR_ARG, "in and out fields must have the same dtype");
-  if (in->dat == out->dat && in->step == out->step) {
-    const size_t lo = in->offset < out->offset ? in->offset : out->offset;
-    const size_t hi = in->offset < out->offset ? out->offset : in->offset;
-    if (hi - lo < (size_t)L.size()) return fail(BK_ERR_ARG, "in and out fields overlap");
-  }
+  if ((s = check_disjoint(in, out, (size_t)L.size()))) return s;
   if ((s = analyze(st, L, plan, tp))) return s;
   if (plan->shape < 0) return fail(BK_ERR_UNSUPPORTED, "brick dims must be 8x8x8, 4x4x4, 16x8x8 or 8x8x32");
   plan->dtype = in->dtype;
@@ -202,6 +198,12 @@ static int prepare(const unsigned *adj, unsigned nbricks, const bk_field *in, co
   if (!err) return fail(BK_ERR_CUDA, "device error word unavailable");
   *a = SweepArgs{adj, nbricks, in->dat, in->step, in->offset, in->chunks,
                  out->dat, out->step, out->offset, out->chunks, blist, 0, err, L};
+  // test hook: make one bounded wait of the TMA star kernel run out (5 ms limit), so that the
+  // timeout path -- flag, stop, drain -- can be exercised; never set in normal use
+  if (plan->tma && !tma_row(*plan) && getenv("BK_TEST_WITHHOLD_COPY")) {
+    a->withhold = 1;
+    a->wait_ns = 5000000ull;
+  }
   return BK_OK;
 }
 

@@ -86,15 +86,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
   return t;
 }
-// Wait for the phase of the given parity to complete; gives up after about one second.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+// Wait for the phase of the given parity to complete; gives up after limit_ns (about one
+// second by default).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity,
+                                                  unsigned long long limit_ns = 1000000000ull) {
   unsigned long long t0 = 0;
   for (unsigned n = 0;; ++n) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((n & 63u) == 63u) {
       const unsigned long long t = global_ns();
       if (!t0) t0 = t;
-      else if (t - t0 > 1000000000ull) return false;
+      else if (t - t0 > limit_ns) return false;
     }
   }
 }
@@ -302,6 +304,7 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
   const long long g0 = blockIdx.x, gstep = gridDim.x;
   const int lane = threadIdx.x & 31;
+  const unsigned long long lim = a.wait_ns ? a.wait_ns : 1000000000ull;
 
   if (threadIdx.x >= C::NC) {
     // ------------------------------------------------------------------ producer warp
@@ -340,7 +343,7 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     unsigned ph = 0;  // (it / S) & 1
     for (long long g = g0; g < ngroups; g += gstep, ++it) {
       // every lane waits (acquire), the warp agrees on the outcome
-      const bool freed = it < S || mbar_wait_bounded(empty0 + 8 * st, ph ^ 1u);
+      const bool freed = it < S || mbar_wait_bounded(empty0 + 8 * st, ph ^ 1u, lim);
       if (!__all_sync(0xFFFFFFFFu, freed)) {
         if (lane == 0) atomicOr(a.err, FLAG_TIMEOUT);
         *abort_word = 1;
@@ -369,7 +372,9 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
       const unsigned bar = full0 + 8 * st;
       if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)__popc(m) * (unsigned)C::TX);
       __syncwarp();
-      if (prod && bact)
+      // the test hook withholds the i-hi copy of the first brick of this CTA's first stage
+      const bool withheld = a.withhold && blockIdx.x == 0 && it == 0 && pbs == 0 && prg == 6;
+      if (prod && bact && !withheld)
       {
         if (pmap == 3) tma_load_4d(sbase + (st * NB + pbs) * C::BRICK + poff, &maps.m[3], px, 0, 0, (int)v, bar);
         else tma_load_3d(sbase + (st * NB + pbs) * C::BRICK + poff, &maps.m[pmap], px, py, (int)v, bar);
@@ -384,10 +389,12 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
         prefetch_l2(in_bytes + (size_t)pf * a.in_step * C::ES, (unsigned)(BK * BJ * BI * C::ES));
       pf = load_pf(g + (PF + 1) * gstep);
     }
-    // copies of the last S issued iterations may still be in flight after an abort
+    // copies of the last S issued iterations may still be in flight after an abort: wait for
+    // each of those stages (bounded; a stage whose wait runs out has had the whole limit for
+    // its copies to land)
     if (lane == 0)
       for (int q = it - S > 0 ? it - S : 0; q < it; ++q)
-        if (!mbar_wait_bounded(full0 + 8 * (q % S), (unsigned)(q / S) & 1u)) break;
+        mbar_wait_bounded(full0 + 8 * (q % S), (unsigned)(q / S) & 1u, lim);
     return;
   }
 
@@ -418,7 +425,7 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
   int st = 0;
   unsigned ph = 0;  // phase parity of the stage's current use
   for (long long g = g0; g < ngroups; g += gstep) {
-    const bool ok = __all_sync(0xFFFFFFFFu, mbar_wait_bounded(full0 + 8 * st, ph));
+    const bool ok = __all_sync(0xFFFFFFFFu, mbar_wait_bounded(full0 + 8 * st, ph, lim));
     if (!ok) {
       atomicOr(a.err, FLAG_TIMEOUT);
       *abort_word = 1;

@@ -251,10 +251,9 @@ int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const b
     return fail(BK_ERR_ARG, "field: offset + brick size exceeds step");
   if (in->dtype != out->dtype || (in->dtype != BK_F64 && in->dtype != BK_F32))
     return fail(BK_ERR_UNSUPPORTED, "4-D sweeps: FP64 or FP32 storage, the same for in and out");
-  if (in->dat == out->dat && in->step == out->step) {
-    const size_t lo = in->offset < out->offset ? in->offset : out->offset;
-    const size_t hi = in->offset < out->offset ? out->offset : in->offset;
-    if (hi - lo < 256) return fail(BK_ERR_ARG, "in and out fields overlap");
+  {
+    const int s_ = check_disjoint(in, out, 256);
+    if (s_) return s_;
   }
   if (st->npoints < 1 || st->npoints > BK_MAX_TAPS4) return fail(BK_ERR_ARG, "4-D stencil npoints out of range");
   int r = 0;

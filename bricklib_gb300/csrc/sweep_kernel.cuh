@@ -58,6 +58,12 @@ struct SweepArgs {
   const uint2 *work;
   unsigned ndom;
   int parity;
+  // bounded waits of the TMA-fed kernels give up after wait_ns (0: one second)
+  unsigned long long wait_ns;
+  // test hook (BK_TEST_WITHHOLD_COPY): the TMA star kernel's first CTA posts its first
+  // stage's byte count but never issues one of that stage's copies, so that stage's wait runs
+  // out; nothing is left in flight.  Zero in normal use.
+  int withhold;
 };
 
 // Taps with a packed-FP32 coefficient pair (every star up to radius 5).

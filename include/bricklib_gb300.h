@@ -300,8 +300,10 @@ int bk_field_norms(const bk_field *a, const bk_field *ref, const unsigned *blist
  * sum of the sums).  Calls no cudaMalloc / cudaFree.  The first call on a device looks up
  * the array's device address (cudaGetSymbolAddress) for that device; make that first call
  * before any stream capture.  All calls share the array and it keeps the last call's
- * contents: calls whose work overlaps on the GPU race.  Synchronises the stream; returns
- * BK_ERR_BOUNDS when a listed brick was out of range. */
+ * contents: calls whose work overlaps on the GPU race.  Synchronises the stream.  One
+ * difference from bk_field_norms: a listed brick out of range (skipped, never read) makes
+ * this call return BK_ERR_BOUNDS itself, where bk_field_norms returns BK_OK and raises the
+ * bounds bit of bk_error_flags. */
 #define BK_NORMS_NOALLOC_MAX_BRICKS 16384
 int bk_field_norms_noalloc(const bk_field *a, const bk_field *ref, const unsigned *blist, unsigned nlist,
                            const bk_layout *lay, void *stream, double out[4]);

@@ -22,16 +22,32 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
 _l3 = C.c_long * 3
 _i3 = C.c_int * 3
+
+
+def reference_tree() -> Optional[str]:
+    """The bricklib source tree the ``ref`` recipe compiles: $BRICKLIB_REF, else the
+    Makefile's default; None where that tree is absent (e.g. on a machine that only runs
+    the prebuilt files)."""
+    path = os.environ.get("BRICKLIB_REF")
+    if not path:
+        try:
+            path = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True,
+                                  check=True).stdout.strip()
+        except (OSError, subprocess.CalledProcessError):
+            return None
+    return path if path and os.path.isdir(os.path.join(path, "include")) else None
 
 
 def build(force: bool = False) -> None:
     """Compile liboracle.so (and _ref/ when the reference tree is present)."""
     if force or not os.path.exists(LIB_PATH):
         subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    if os.path.isdir("/root/reference/include") and (force or not os.path.exists(REF_PATH)):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+    tree = reference_tree()
+    if tree and (force or not os.path.exists(REF_PATH)):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={tree}"])
 
 
 _lib = None
@@ -84,6 +100,10 @@ def ref() -> Optional[C.CDLL]:
         R.ref_layout_offsets4.argtypes = [C.c_int, _i64p]
         R.ref_init_grid4.argtypes = [C.c_long, C.c_long, C.c_long, C.c_long, _u32p, _u32p]
         R.ref_sweep4.argtypes = [C.c_int, C.c_long, _f64p, C.c_int, _i32p, _f64p, _f64p, _f64p]
+        R.ref_skin_list.argtypes = [C.c_int, C.c_void_p]
+        R.ref_allneighbors.argtypes = [C.c_int, C.c_void_p]
+        R.ref_decomp.argtypes = [C.c_int, _u32p, C.c_uint, C.c_uint, C.c_long, C.c_long, _u64p, C.c_uint, _i64p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _ref = R
     return _ref
 

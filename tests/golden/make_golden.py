@@ -14,6 +14,9 @@ Fixtures written:
   sweep4_<name>.npz one 4-D sweep on an 8^4 interior (ghost 8, padding 4, weak/main-4d.cpp):
                     mpi9pt (stencils/mpi9pt.py, alpha 0.2 / beta 0.1) with fold (2,4) and fold (1),
                     and a 9-point star with seeded coefficients; input uniform[-1,1) seed 1234
+  decomp_<case>.npz the reference's BrickDecomp layouts (grid, adjacency, g_region records, skin
+                    sizes) for the cases of DECOMP_CASES; decomp_skin_lists.npz its skin orders
+                    and allneighbors order (`--decomp` writes only these)
   sweep_<shape>.npz one sweep on a 16^3 interior (sweep_cond7: the reference's cond kernel,
                     |sum coeff * max(x, 0)|, stencils/3axis.cpp:94-163) (+8 ghost, +8 padding) through
                     copyToBrick -> accessor brick kernel -> compareBrick -> copyFromBrick,
@@ -133,5 +136,72 @@ def main():
         print(f"{'4d ' + name:22s} compareBrick={ok} max|brick-array|={np.max(np.abs(ob - oa)):.3e}")
 
 
+# BrickDecomp cases: (name, bcase of ref_decomp, dims contiguous first, brick dims, depth,
+# numfield, element bytes, page bytes, skin list); bcase 0 <3,8,8,8>, 1 <3,4,4,4>, 2 <2,8,8>,
+# 3 <4,4,4,4,4>.  Skin lists: "good" / "normal" are the reference's skin3d_good / skin3d_normal,
+# "all" its allneighbors order without the empty region.
+DECOMP_CASES = [
+    ("good_f1", 0, (32, 32, 32), (8, 8, 8), 8, 1, 8, 4096, "good"),
+    ("good_f2_aniso", 0, (32, 24, 40), (8, 8, 8), 8, 2, 8, 4096, "good"),
+    ("good_e4_padded", 0, (32, 32, 32), (8, 8, 8), 8, 1, 4, 4096, "good"),
+    ("normal_e2_ghost2", 0, (48, 32, 32), (8, 8, 8), 16, 1, 2, 4096, "normal"),
+    ("good_unpadded", 0, (32, 32, 32), (8, 8, 8), 8, 1, 8, 1, "good"),
+    ("good_unpadded_f2", 0, (40, 32, 24), (8, 8, 8), 8, 2, 8, 1, "good"),
+    ("good_b4", 1, (16, 16, 16), (4, 4, 4), 4, 1, 8, 4096, "good"),
+    ("all2d", 2, (32, 32), (8, 8), 8, 1, 8, 4096, "all"),
+    ("all4d", 3, (16, 16, 16, 16), (4, 4, 4, 4), 8, 1, 8, 4096, "all"),
+]
+
+
+def decomp_main():
+    """decomp_<name>.npz: the reference's own BrickDecomp<dim, bdim>(dims, depth, numfield)
+    .initialize(skin) (include/brick-mpi.h:298-464, oracle/ref_decomp.cpp): nbricks, sep_pos,
+    the grid (position -> brick, dimension 0 fastest), the adjacency, the ghost and skin g_region
+    records (7 int64 each) and the skin sizes; plus the skin lists it was given."""
+    oracle.build()
+    R = oracle.ref()
+    if R is None:
+        raise SystemExit("reference checker not built (needs the reference tree)")
+    lists = {}
+    for which, key in ((0, "good"), (1, "normal")):
+        n = R.ref_skin_list(which, None)
+        a = np.zeros(n, np.uint64)
+        R.ref_skin_list(which, a.ctypes.data)
+        lists[key] = a
+    for dim in (2, 3, 4):
+        n = R.ref_allneighbors(dim, None)
+        a = np.zeros(n, np.uint64)
+        R.ref_allneighbors(dim, a.ctypes.data)
+        lists[f"neighbors{dim}"] = a
+    np.savez(os.path.join(OUT, "decomp_skin_lists.npz"), **lists)
+    for name, bcase, dims, bdim, depth, nf, eb, page, skin in DECOMP_CASES:
+        dim = len(dims)
+        sk = lists[skin] if skin != "all" else lists[f"neighbors{dim}"]
+        sk = np.ascontiguousarray(sk[sk != 0] if skin == "all" else sk, np.uint64)
+        dv = np.asarray(dims, np.uint32)
+        info = np.zeros(6, np.int64)
+        assert R.ref_decomp(bcase, dv, depth, nf, eb, page, sk, len(sk), info, None, None, None, None) == 0
+        nb, gsize, nreg = int(info[0]), int(info[4]), int(info[5])
+        grid = np.zeros(gsize, np.uint32)
+        adj = np.zeros(nb * 3 ** dim, np.uint32)
+        regions = np.zeros(2 * nreg * 7, np.int64)
+        skin_size = np.zeros(len(sk), np.int64)
+        assert R.ref_decomp(bcase, dv, depth, nf, eb, page, sk, len(sk), info, grid.ctypes.data, adj.ctypes.data,
+                            regions.ctypes.data, skin_size.ctypes.data) == 0
+        # initialize writes the adjacency rows of the bricks the grid holds (brick-mpi.h:460-463);
+        # rows of reserved and page-padding bricks stay as allocated (uninitialised): recorded as 0
+        adj = adj.reshape(nb, 3 ** dim)
+        unused = np.setdiff1d(np.arange(nb), grid)
+        adj[unused] = 0
+        np.savez_compressed(os.path.join(OUT, f"decomp_{name}.npz"), dims=dv, bdim=np.asarray(bdim), depth=depth,
+                            numfield=nf, elem_bytes=eb, pagesize=page, skinlist=sk, nbricks=nb,
+                            sep_pos=info[1:4].copy(), grid=grid, adj=adj, unused=unused,
+                            ghost=regions[:7 * nreg].reshape(nreg, 7), skin=regions[7 * nreg:].reshape(nreg, 7),
+                            skin_size=skin_size)
+        print(f"decomp {name:18s} nbricks={nb} sep_pos={info[1:4].tolist()} regions={nreg}")
+
+
 if __name__ == "__main__":
-    main()
+    if "--decomp" not in sys.argv:
+        main()
+    decomp_main()

@@ -5,9 +5,11 @@ import numpy as np
 import pytest
 
 from bricklib_gb300 import dsl, stencils
+from oracle import oracle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference/stencils"
+_TREE = oracle.reference_tree()  # $BRICKLIB_REF or the oracle recipe's default; None when absent
+REF = os.path.join(_TREE, "stencils") if _TREE else ""
 
 
 def test_loop_script_lowers_to_star13():

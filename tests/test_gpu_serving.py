@@ -59,6 +59,43 @@ def test_fp64_job_matches_oracle():
     assert np.abs(out[0] - want).max() <= 1e-12 * np.abs(want).max()
 
 
+def oracle_periodic_steps(j, st, inp):
+    """The oracle's array path with periodic fill, FP64, from the job's (rounded) input."""
+    n = j.n
+    dom = oracle.Domain(n)
+    o = dom.ghost + dom.pad
+    a = np.zeros(dom.adims)
+    a[o:o + n[0], o:o + n[1], o:o + n[2]] = inp
+    b = np.zeros_like(a)
+    for _ in range(j.steps):
+        oracle.array_periodic_fill(a, (o,) * 3, n, (8, 8, 8))
+        oracle.array_sweep(a, b, (o,) * 3, tuple(o + x for x in n), st.offsets(), st.coeff)
+        a, b = b, a
+    return a[o:o + n[0], o:o + n[1], o:o + n[2]]
+
+
+def test_fp32_jobs_in_a_mix_match_the_fp64_oracle():
+    """Served FP32 jobs (FP32 storage, FP32 arithmetic), one of each shape, submitted together with
+    FP64 jobs: each result is within 1e-5 normwise (max |d| / max |ref|) of the FP64 oracle run from
+    the same FP32-rounded input, and every FP64 job within 1e-12."""
+    jobs = [serving.JobSpec((24, 16, 32), "star7", 12, BK_F32, 201),
+            serving.JobSpec((16, 32, 24), "star13", 9, BK_F32, 202),
+            serving.JobSpec((32, 24, 16), "star25", 6, BK_F32, 203),
+            serving.JobSpec((24, 24, 24), "cube27", 8, BK_F32, 204),
+            serving.JobSpec((16, 24, 32), "cube125", 5, BK_F32, 205),
+            serving.JobSpec((24, 16, 16), "cube125", 4, BK_F64, 206),
+            serving.JobSpec((16, 16, 24), "star25", 3, BK_F64, 207)]
+    out, st, _ = run(jobs)
+    assert st["completed"] == len(jobs)
+    for j, got in zip(jobs, out):
+        inp = stencils.uniform(j.seed, j.points).reshape(j.n)
+        if j.dtype == BK_F32:
+            inp = inp.astype(np.float32).astype(np.float64)
+        want = oracle_periodic_steps(j, stencils.make(j.shape, 5), inp)
+        err = float(np.abs(got.astype(np.float64) - want).max() / np.abs(want).max())
+        assert err <= (1e-5 if j.dtype == BK_F32 else 1e-12), (j, err)
+
+
 def test_budget_gates_admission_and_rejects_oversized_jobs():
     jobs = small_jobs()
     one = max(j.points for j in jobs) * 8 * 6  # room for about one job at a time

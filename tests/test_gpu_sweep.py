@@ -600,3 +600,34 @@ def test_dsl_script_runs_on_the_gpu():
     dom, arr, got = device_sweep(32, st, seed=21)
     ok, md = mixed_ok(got, oracle_array(dom, arr, st))
     assert ok, md
+
+
+def test_a_bounded_wait_that_runs_out_is_flagged_and_the_device_stays_usable(monkeypatch):
+    """The TMA star kernel's waits are bounded.  With the test hook BK_TEST_WITHHOLD_COPY its
+    first CTA posts a stage's byte count but withholds one of that stage's copies (so no copy is
+    left in flight) and the wait limit drops to 5 ms: the consumers' wait runs out, the CTA sets
+    the timeout flag, stops, and its producer drains its stages with bounded waits.  The host
+    reads BK_ERR_TIMEOUT from the flags; the next sweep is clean and matches the oracle."""
+    monkeypatch.delenv("BK_SWEEP_ONESHOT", raising=False)
+    monkeypatch.delenv("BK_SWEEP_PIPELINED", raising=False)
+    st = stencils.make("star7", 7)
+    dom = GridDomain(64)
+    arr = stencils.uniform(77, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    assert B.sweepKernel(dom.brick(0), dom.brick(1), st) == "sweep_star_tma_kernel"
+    B.check_device()
+    monkeypatch.setenv("BK_TEST_WITHHOLD_COPY", "1")
+    B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, st)
+    B.synchronize()
+    with pytest.raises(_abi.BkError) as e:
+        B.check_device()
+    assert e.value.status == _abi.BK_ERR_TIMEOUT
+    assert B.error_flags() == 0  # read and cleared
+    monkeypatch.delenv("BK_TEST_WITHHOLD_COPY")
+    B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, st)
+    B.synchronize()
+    B.check_device()
+    dom.download()
+    ok, md = mixed_ok(dom.interior_view(dom.get_field(1)), oracle_array(dom, arr, st))
+    assert ok, f"max |diff| {md}"

@@ -100,6 +100,48 @@ def test_kernel_choice(monkeypatch):
     assert _kernel_for("star7") == "sweep_kernel"
 
 
+def test_in_and_out_fields_that_alias_are_rejected():
+    """A sweep never writes an element it reads: one storage seen with two steps, or two
+    storages whose bytes overlap, is rejected before any launch (3-D and 4-D); the interleaved
+    bIn / bOut of one storage (offsets a brick apart) and separate storages are accepted."""
+    from bricklib_gb300 import bricks4 as B4
+    lay = B.Layout()
+    size, base = lay.size, 1 << 20
+    cst = B.to_c_stencil(stencils.make("star7", 1))
+
+    def kernel(fin, fout):
+        out = C.c_char_p()
+        return _abi.lib().bk_sweep_kernel(C.byref(fin), C.byref(fout), C.byref(cst), C.byref(lay.to_c()),
+                                          _abi.BK_ACC_NATIVE, C.byref(out))
+
+    f = _abi.bk_field
+    ok_pairs = [
+        (f(C.c_void_p(base), 100, 2 * size, 0, _abi.BK_F64), f(C.c_void_p(base), 100, 2 * size, size, _abi.BK_F64)),
+        (f(C.c_void_p(base), 100, size, 0, _abi.BK_F64), f(C.c_void_p(base + 100 * size * 8), 100, size, 0, _abi.BK_F64)),
+    ]
+    bad_pairs = [
+        # one storage, two steps: brick b of one field meets brick b' of the other
+        (f(C.c_void_p(base), 100, 2 * size, 0, _abi.BK_F64), f(C.c_void_p(base), 100, 3 * size, size, _abi.BK_F64)),
+        # two storages overlapping in memory
+        (f(C.c_void_p(base), 100, size, 0, _abi.BK_F64), f(C.c_void_p(base + 50 * size * 8), 100, size, 0, _abi.BK_F64)),
+        # one storage, offsets less than a brick apart
+        (f(C.c_void_p(base), 100, 2 * size, 0, _abi.BK_F64), f(C.c_void_p(base), 100, 2 * size, 8, _abi.BK_F64)),
+    ]
+    for a, b in ok_pairs:
+        assert kernel(a, b) == 0, _abi.lib().bk_last_error()
+    for a, b in bad_pairs:
+        assert kernel(a, b) == _abi.BK_ERR_ARG
+        assert b"overlap" in _abi.lib().bk_last_error() or b"share storage" in _abi.lib().bk_last_error()
+    # 4-D: the same rule (nlist 0, so nothing would launch even if the fields were accepted)
+    st4 = B4.to_c_stencil4(B4.mpi9pt())
+    lay4 = B4.Layout4().to_c()
+    good4 = (f(C.c_void_p(base), 100, 512, 0, _abi.BK_F64), f(C.c_void_p(base), 100, 512, 256, _abi.BK_F64))
+    bad4 = (f(C.c_void_p(base), 100, 512, 0, _abi.BK_F64), f(C.c_void_p(base), 100, 768, 256, _abi.BK_F64))
+    for (a, b), want in ((good4, 0), (bad4, _abi.BK_ERR_ARG)):
+        got = _abi.lib().bk_sweep4(None, 0, C.byref(a), C.byref(b), None, 0, C.byref(st4), C.byref(lay4), None)
+        assert got == want, _abi.lib().bk_last_error()
+
+
 def test_stencil_errors_are_reported_not_raised_in_c():
     bad = stencils.custom("far", [(0, 0, 9)], [1.0])
     with pytest.raises(_abi.BkError) as e:

@@ -59,6 +59,37 @@ def test_noalloc_norms_match_allocating_norms_twice():
     assert got2 != got1
 
 
+def test_noalloc_norms_report_an_out_of_range_brick_then_recover():
+    """A listed brick past the storage is skipped (never read) and this call returns
+    BK_ERR_BOUNDS; the error word is private to the call, so the next in-range call returns 0
+    with the norms of bk_field_norms.  Device memory in use is the same before and after the
+    calls: nothing was allocated."""
+    import torch
+    dom = GridDomain(32)
+    arr = stencils.uniform(43, int(np.prod(dom.adims))).reshape(dom.adims)
+    dom.set_field(0, arr)
+    dom.upload()
+    B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, stencils.make("star13", 4))
+    B.synchronize()
+    norms("bk_field_norms_noalloc", dom.brick(1), dom.brick(0), dom.dev_interior)  # first call on this device
+    bad = B.BrickList(np.concatenate([dom.interior[:5], [dom.nbricks + 7], dom.interior[5:9]]).astype(np.uint32))
+    status, _ = norms("bk_field_norms_noalloc", dom.brick(1), dom.brick(0), bad)
+    assert status == _abi.BK_ERR_BOUNDS
+    assert "out of range" in _abi.lib().bk_last_error().decode()
+    s_ok, got = norms("bk_field_norms_noalloc", dom.brick(1), dom.brick(0), dom.dev_interior)
+    r_ok, want = norms("bk_field_norms", dom.brick(1), dom.brick(0), dom.dev_interior)
+    assert s_ok == 0 and r_ok == 0 and close(got, want), (got, want)
+    B.synchronize()
+    # bk_field_norms keeps a buffer made on its first call, and the list above is a device
+    # buffer; from here on only no-alloc calls run, and free device memory must not move
+    free1, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        s_again, _ = norms("bk_field_norms_noalloc", dom.brick(1), dom.brick(0), dom.dev_interior)
+        assert s_again == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free1
+
+
 def test_noalloc_norms_reject_lists_beyond_the_static_maximum():
     dom = GridDomain(16)
     big = B.BrickList(np.zeros(MAX_BRICKS + 1, dtype=np.uint32))
