@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-alt", action="store_true")
+    p.add_argument("--no-forms", action="store_true")
     p.add_argument("--ndom", type=int, default=256)
     p.add_argument("--rates", default="200,2000")
     p.add_argument("--njobs", type=int, default=400)
@@ -388,18 +389,19 @@ def run_ours(args):
         cpu = cpu_baseline_on_device_data(B, s_in, s_out, info, interior, sts, shapes, lay, nbricks, bsize, sp,
                                           lambda name: (sweep(name), torch.cuda.synchronize()))
 
+    forms = None
+    if rank == 0 and not args.no_forms and args.n == 512 and dtype == _abi.BK_F64:
+        forms = forms_record(args)
+
     if rank == 0:
         line = {"metric": "GStencil/s", "value": round(value, 3), "unit": "GStencil/s", "n_gpus": ws,
                 "steps": K, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": {"f64": "f64", "f32": "f32", "bf16": "bf16"}[args.dtype],
                 "data": "synthetic: seeded uniform[-1,1) input, seeded coefficients normalised to sum 1",
-                "config": {"workload": f"plain {args.dtype} brick sweep, {n}^3 interior + 8-cell ghost, 8x8x8 bricks "
-                                       f"fold (4,8), one sweep each of {'/'.join(shapes)}",
-                           "interior_points": points, "bricks": nbricks, "accumulation": args.acc,
-                           "l2": f"no flush: inputs {nbricks * bsize * esize / 1e9:.2f} GB per field > 129 MB L2",
-                           "parallelism": f"replicas x{ws}"},
+                "config": plain_config(args, shapes, nbricks, esize, ws),
                 "per_stencil": per_shape, "alt_mode": alt, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "forms": forms,
                 "gpu_launches": K * len(shapes), "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -429,53 +431,107 @@ def fp_instructions_per_point(st, acc, dtype=None) -> float:
     return {(1, False): 18.25, (1, True): 16.5, (2, False): 69.0, (2, True): 58.5}[(r, ij)]
 
 
+def cpu_info(threads: int) -> dict:
+    """The host the CPU leg ran on: core counts, CPU model and the OpenMP settings."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    try:
+        affinity = len(os.sched_getaffinity(0))
+    except AttributeError:
+        affinity = os.cpu_count()
+    return {"nproc": os.cpu_count(), "affinity": affinity, "threads_used": threads, "model": model or "unknown",
+            "OMP_NUM_THREADS": os.environ.get("OMP_NUM_THREADS", "unset"),
+            "OMP_PROC_BIND": os.environ.get("OMP_PROC_BIND", "unset")}
+
+
+def plain_config(args, shapes, nbricks: int, esize: int, ws: int) -> dict:
+    """The plain-form workload, identical in both arms' lines."""
+    n = args.n
+    return {"workload": f"plain {args.dtype} brick sweep, {n}^3 interior + 8-cell ghost, 8x8x8 bricks fold (4,8), "
+                        f"one sweep each of {'/'.join(shapes)}",
+            "interior_points": n ** 3, "bricks": nbricks, "accumulation": args.acc,
+            "l2": (f"no flush: inputs {nbricks * 512 * esize / 1e9:.2f} GB per field > 129 MB L2"
+                   if nbricks * 512 * esize > 129e6 else
+                   f"inputs {nbricks * 512 * esize / 1e6:.1f} MB per field fit in L2: a small case, not a bench value"),
+            "parallelism": f"replicas x{ws}"}
+
+
+CPU_BUILD = ("the oracle's OpenMP brick sweep (gather of the rows the taps read, then taps in order per row), "
+             "built as the reference builds its CPU path: gcc -O2 -fopenmp with default floating-point "
+             "contraction (oracle/Makefile, target timed)")
+
+
+def cpu_plain_steps(oracle, adj, host_in, out, interior, sts, shapes, steps: int, warmup: int, threads: int):
+    """`warmup` then `steps` CPU steps of the plain workload (one sweep of each shape over every
+    interior brick, separate input and output storages, as the GPU arm runs it); per-shape
+    mean seconds and mean seconds per step."""
+    per = {name: 0.0 for name in shapes}
+    for it in range(warmup + steps):
+        for name in shapes:
+            st = sts[name]
+            t = time.perf_counter()
+            oracle.brick_sweep(adj, host_in, 512, 0, out, 512, 0, interior, (8, 8, 8), (1, 4, 8), st.offsets(),
+                               st.coeff, threads, timed=True)
+            if it >= warmup:
+                per[name] += time.perf_counter() - t
+    per = {k: v / steps for k, v in per.items()}
+    return per, sum(per.values())
+
+
 def cpu_baseline_on_device_data(B, s_in, s_out, info, interior, sts, shapes, lay, nbricks, bsize, sp, run_one):
+    """The CPU leg of this arm: the same workload on the host cores (one untimed and two timed
+    steps, ~10 s on 16 cores), from the device input; every interior point of every GPU result
+    is then compared with the CPU result (normwise)."""
     from oracle import oracle
     host_in = np.empty(nbricks * bsize, dtype=np.float64)
     B.memcpy(host_in.ctypes.data, s_in.ptr, host_in.nbytes, 1, sp)
     B.synchronize(sp)
     adj = np.ascontiguousarray(info.adj.reshape(-1))
     threads = oracle.max_threads()
-    rng = np.random.default_rng(1)
-    res = {}
-    total_pts, total_s = 0, 0.0
+    out = np.zeros(nbricks * bsize, dtype=np.float64)
+    per, step_s = cpu_plain_steps(oracle, adj, host_in, out, interior, sts, shapes, 2, 1, threads)
+    points = len(interior) * bsize
     max_err = 0.0
+    gpu = np.empty(nbricks * bsize, dtype=np.float64)
+    rows = interior.astype(np.int64)
     for name in shapes:
         st = sts[name]
-        # ~2 s of CPU work per shape at the expected rate
-        rate = 2e9 / st.flops_per_point * threads / 8  # points/s guess
-        m = int(min(len(interior), max(64, 2.0 * rate / bsize)))
-        sample = np.ascontiguousarray(np.sort(rng.choice(interior, size=m, replace=False)), dtype=np.uint32)
-        out = np.zeros(nbricks * bsize, dtype=np.float64)
-        # repeat the sweep of the sample until it has run for at least 2 s (the whole interior is
-        # the sample when it fits that budget)
-        reps, dt = 0, 0.0
-        while dt < 2.0:
-            t = time.perf_counter()
-            oracle.brick_sweep(adj, host_in, bsize, 0, out, bsize, 0, sample, lay.bdim, lay.fold, st.offsets(),
-                               st.coeff, threads)
-            dt += time.perf_counter() - t
-            reps += 1
-        total_pts += reps * m * bsize
-        total_s += dt
-        res[name] = round(reps * m * bsize / dt / 1e9, 4)
-        # spot check against the GPU result for the same bricks
+        oracle.brick_sweep(adj, host_in, bsize, 0, out, bsize, 0, interior, lay.bdim, lay.fold, st.offsets(),
+                           st.coeff, threads, timed=True)
         run_one(name)
-        gpu = np.empty(nbricks * bsize, dtype=np.float64)
         B.memcpy(gpu.ctypes.data, s_out.ptr, gpu.nbytes, 1, sp)
         B.synchronize(sp)
-        idx = (sample[:, None].astype(np.int64) * bsize + np.arange(bsize)[None, :]).reshape(-1)
-        a, b = gpu[idx], out[idx]
+        a, b = gpu.reshape(-1, bsize)[rows], out.reshape(-1, bsize)[rows]
         max_err = max(max_err, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
-    return {"value": round(total_pts / total_s / 1e9, 4), "unit": "GStencil/s", "cores": threads, "kind": "port",
-            "sample": f"oracle OpenMP brick sweep of up to {len(interior)} interior bricks per shape, repeated "
-                      f"for >= 2 s each: {total_pts} points in {total_s:.1f} s",
-            "per_stencil": res, "gpu_vs_oracle_max_normwise_err": max_err}
+    return {"value": round(len(shapes) * points / step_s / 1e9, 4), "unit": "GStencil/s", "cores": threads,
+            "kind": "port",
+            "sample": f"the whole workload ({len(shapes)} sweeps of {points} interior points per step), one untimed "
+                      f"and two timed steps, {step_s:.2f} s per step; {CPU_BUILD}",
+            "per_stencil": {k: round(points / v / 1e9, 4) for k, v in per.items()},
+            "host": cpu_info(threads), "gpu_vs_cpu_max_normwise_err": max_err}
 
 
 # ---------------------------------------------------------------------------- reference arm
 
 def run_reference(args):
+    """The reference's CPU brick path on the host cores, on this arm's workload and config: the
+    same 512^3 input (the splitmix64 stream the device fill writes), the same bricks, fold, taps
+    and separate input / output storages; each step one sweep of each shape."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
@@ -483,40 +539,26 @@ def run_reference(args):
     from oracle import oracle
     oracle.build()
     shapes = args.shapes.split(",")
-    # the reference's CPU brick path, timed on a 256^3-interior sample of the workload per
-    # shape per step (same bricks, fold and taps; large enough that the OpenMP brick loop, not
-    # the per-call overhead, sets the rate; the reference-compiled build does not travel to an
-    # aarch64 host, so the OpenMP restatement of it runs here)
-    m = 256
-    dom = oracle.Domain(m)
-    arr = stencils.uniform(SEED_IN, int(np.prod(dom.adims))).reshape(dom.adims)
-    dat = dom.alloc()
-    dom.to_bricks(arr, dat, 0)
+    n = args.n
+    g = n // 8 + 2
+    grid, adj = oracle.init_grid(g, g, g)
+    nbricks = g ** 3
+    interior = np.ascontiguousarray(grid.reshape(g, g, g)[1:-1, 1:-1, 1:-1].reshape(-1))
+    host_in = oracle.fill_uniform(nbricks * 512, SEED_IN)
+    out = np.zeros(nbricks * 512)
     threads = oracle.max_threads()
     sts = {name: stencils.make(name, SEED_COEFF) for name in shapes}
-
-    def step():
-        for name in shapes:
-            st = sts[name]
-            oracle.brick_sweep(dom.adj, dat, dom.step, 0, dat, dom.step, dom.bsize, dom.interior, dom.bdim, dom.fold,
-                               st.offsets(), st.coeff, threads)
-
-    for _ in range(args.warmup):
-        step()
-    t = time.perf_counter()
-    for _ in range(args.steps):
-        step()
-    dt = (time.perf_counter() - t) / args.steps
-    value = len(shapes) * m ** 3 / dt / 1e9
+    per, step_s = cpu_plain_steps(oracle, adj, host_in, out, interior, sts, shapes, args.steps, args.warmup, threads)
+    value = len(shapes) * n ** 3 / step_s / 1e9
+    cpu = {"value": round(value, 4), "unit": "GStencil/s", "cores": threads, "kind": "port",
+           "sample": f"the whole workload, {args.warmup} untimed and {args.steps} timed steps; {CPU_BUILD}",
+           "per_stencil": {k: round(n ** 3 / v / 1e9, 4) for k, v in per.items()}, "host": cpu_info(threads)}
     line = {"impl": "reference", "metric": "GStencil/s", "value": round(value, 4), "unit": "GStencil/s",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3),
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded uniform[-1,1) input, seeded coefficients normalised to sum 1",
-            "config": {"workload": f"plain f64 brick sweep, {args.n}^3 interior + 8-cell ghost, 8x8x8 bricks, "
-                                   f"one sweep each of {'/'.join(shapes)}",
-                       "sample": f"{m}^3 interior per shape per step"},
-            "cpu_baseline": {"value": round(value, 4), "unit": "GStencil/s", "cores": threads, "kind": "port",
-                             "sample": f"{m}^3 interior (+ghost) per shape per step, OpenMP brick sweep of the oracle"},
+            "config": plain_config(args, shapes, nbricks, 8, ws),
+            "cpu_baseline": cpu,
             "e2e": {"value": round(value, 4), "unit": "GStencil/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -538,28 +580,31 @@ def run_precision(args):
                           "reference": "FP64 native run on the device", "records": recs}), flush=True)
 
 
-def run_batched(args):
-    """The batched form (256 uneven periodic FP32 domains): autotune the layout, then 10 FP32 steps of all 256
-    domains from one captured graph, against the plain FP64 drop-in run domain by domain (and
-    an unbatched FP32 run), with the FP32 error against FP64."""
+def batched_record(ndom: int, tune: bool, reps: int = 5) -> dict:
+    """The batched form on `ndom` uneven periodic FP32 domains: 10 steps of all domains from one
+    captured graph, against the plain FP64 drop-in run domain by domain and an unbatched FP32
+    run of the same domains (both with their ghost fills), and the FP32 error against FP64.
+    With `tune` the autotuner picks the layout first, else the default 8^3 bricks run."""
     import torch
     from bricklib_gb300 import _abi, batch as BT, bricks as B
     from bricklib_gb300._abi import call
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    call("bk_set_device", local)
     stream = torch.cuda.current_stream()
-    w = BT.make_workload(ndom=args.ndom)
+    w = BT.make_workload(ndom=ndom)
     steps = 10
-    t0 = time.perf_counter()
-    tune = BT.autotune(w, _abi.BK_F32, _abi.BK_ACC_NATIVE, steps=steps, use_cache=False)
-    tune_s = time.perf_counter() - t0
-    best = tune["best"]
-    lay = B.Layout(tuple(best["bdim"]), tuple(best["fold"]))
+    tune_rec = None
+    if tune:
+        t0 = time.perf_counter()
+        res = BT.autotune(w, _abi.BK_F32, _abi.BK_ACC_NATIVE, steps=steps, use_cache=False)
+        best = res["best"]
+        lay, cap = B.Layout(tuple(best["bdim"]), tuple(best["fold"])), best["grid_cap"]
+        tune_rec = {"seconds": round(time.perf_counter() - t0, 1), "table": res["table"]}
+    else:
+        lay, cap = B.DEFAULT_LAYOUT, 0
     bt = BT.Batch(w, lay, _abi.BK_F32)
-    call("bk_batch_set_grid", bt.h, best["grid_cap"])
-    t_batch = BT.time_batch(bt, steps, reps=5)
+    call("bk_batch_set_grid", bt.h, cap)
+    t_batch = BT.time_batch(bt, steps, reps=reps)
     gst_batch = w.points * steps / t_batch / 1e9
+    bt.close()
 
     def unbatched(dtype, lay_):
         tot = 0.0
@@ -579,11 +624,10 @@ def run_batched(args):
             outs.append((ds, lst))
         return tot, outs
 
-    t_plain64, _ = unbatched(_abi.BK_F64, B.DEFAULT_LAYOUT)
-    t_plain32, _ = unbatched(_abi.BK_F32, B.DEFAULT_LAYOUT)
+    t_plain64, outs64 = unbatched(_abi.BK_F64, lay)
+    t_plain32, _ = unbatched(_abi.BK_F32, lay)
     # error of a fresh 10-step batched FP32 run against the per-domain FP64 run of the same
-    # domains on the same layout, domain by domain (the timed batch has run many more steps)
-    _, outs64 = unbatched(_abi.BK_F64, lay)
+    # domains on the same layout, domain by domain
     chk = BT.Batch(w, lay, _abi.BK_F32)
     chk.run(steps, stream=stream.cuda_stream)
     torch.cuda.synchronize()
@@ -592,22 +636,39 @@ def run_batched(args):
         nrm = B.fieldNorms(ds32.field(chk.parity), ds64.field(steps % 2), lst)
         worst = max(worst, nrm["max_rel"])
     chk.close()
+    rec = {"metric": "GStencil/s", "unit": "GStencil/s", "domains": len(w.domains), "interior_points": w.points,
+           "steps": steps,
+           "batched_fp32": {"value": round(gst_batch, 2), "ms_per_10_steps": round(t_batch * 1e3, 3),
+                            "layout": {"bdim": lay.bdim, "fold": lay.fold, "grid_cap": cap,
+                                       "chosen_by": "autotuner" if tune else "default 8^3 bricks"},
+                            "graph": True, "periodic": "through the adjacency (no ghost fill)"},
+           "plain_fp64_per_domain": {"value": round(w.points * steps / t_plain64 / 1e9, 2),
+                                     "ms": round(t_plain64 * 1e3, 2),
+                                     "note": "the drop-in run domain by domain, ghost fill before every step"},
+           "unbatched_fp32_per_domain": {"value": round(w.points * steps / t_plain32 / 1e9, 2),
+                                         "ms": round(t_plain32 * 1e3, 2),
+                                         "note": "the same FP32 arithmetic domain by domain, ghost fill every step"},
+           "batched_vs_plain_fp64": round(t_plain64 / t_batch, 2),
+           "batched_vs_unbatched_fp32": round(t_plain32 / t_batch, 2),
+           "fp32_max_normwise_err_vs_fp64": worst}
+    if tune_rec:
+        rec["autotune"] = tune_rec
+    return rec
+
+
+def run_batched(args):
+    """The batched form (256 uneven periodic FP32 domains), the layout chosen by the autotuner."""
+    import torch
+    from bricklib_gb300._abi import call
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    call("bk_set_device", local)
+    rec = batched_record(args.ndom, tune=True)
     if rank == 0:
-        print(json.dumps({
-            "form": "batched", "metric": "GStencil/s", "unit": "GStencil/s",
-            "domains": len(w.domains), "interior_points": w.points, "steps": steps,
-            "batched_fp32": {"value": round(gst_batch, 2), "ms_per_10_steps": round(t_batch * 1e3, 3),
-                             "layout": {"bdim": lay.bdim, "fold": lay.fold, "grid_cap": best["grid_cap"]},
-                             "graph": True, "periodic": "through the adjacency (no ghost fill)",
-                             "launches_per_step": len({d.stencil for d in w.domains})},
-            "plain_fp64_per_domain": {"value": round(w.points * steps / t_plain64 / 1e9, 2),
-                                      "ms": round(t_plain64 * 1e3, 2)},
-            "unbatched_fp32_per_domain": {"value": round(w.points * steps / t_plain32 / 1e9, 2),
-                                          "ms": round(t_plain32 * 1e3, 2)},
-            "batched_vs_plain": round(t_plain64 / t_batch, 2),
-            "fp32_max_normwise_err_vs_fp64": worst,
-            "autotune": {"seconds": round(tune_s, 1), "table": tune["table"]}}), flush=True)
-    bt.close()
+        print(json.dumps({"form": "batched", **rec}), flush=True)
+
+
+SERVING_JOBS = "edges log-uniform [16,192] (multiples of 8), 5 shapes, steps U[1,200], 50% FP64 / 50% FP32"
 
 
 def run_serving(args):
@@ -627,8 +688,34 @@ def run_serving(args):
             res.append(st)
     if rank == 0:
         print(json.dumps({"form": "serving", "metric": "p50/p99 latency (s), GStencil/s", "budget_bytes": 150e9,
-                          "jobs": "edges log-uniform [16,192] (multiples of 8), 5 shapes, steps U[1,200], "
-                                  "50% FP64 / 50% FP32", "runs": res}), flush=True)
+                          "jobs": SERVING_JOBS, "runs": res}), flush=True)
+
+
+def forms_record(args) -> dict:
+    """The three forms in compact runs (about a minute together), for the default line: the
+    batched form (default bricks, no autotuning), 200 served jobs at 200 and 2000 jobs/s, and the
+    precision form's errors after 1 and 10 steps at 512^3."""
+    import torch
+    from bricklib_gb300 import _abi, precision, serving
+    out = {}
+    t = time.perf_counter()
+    out["batched"] = batched_record(args.ndom, tune=False, reps=3)
+    out["batched"]["seconds"] = round(time.perf_counter() - t, 1)
+    t = time.perf_counter()
+    runs = []
+    for rate in (200.0, 2000.0):
+        st = serving.run_load(rate, 200, fp64_acc=_abi.BK_ACC_NATIVE)
+        runs.append({k: st[k] for k in ("rate", "p50_s", "p99_s", "gstencil_s", "completed") if k in st})
+    out["serving"] = {"jobs": 200, "job_mix": SERVING_JOBS, "budget_bytes": 150e9, "fp64_arithmetic": "native",
+                      "runs": runs, "seconds": round(time.perf_counter() - t, 1)}
+    t = time.perf_counter()
+    recs = precision.run_study(n=512, shapes=("heat7", "cube125"), variants=("f32", "bf16"), steps=(1, 10),
+                               stream=torch.cuda.current_stream().cuda_stream, timing=False)
+    out["precision"] = {"n": 512, "reference": "FP64 native run on the device",
+                        "records": [{k: r[k] for k in ("stencil", "variant", "steps", "max_rel_err", "rms_rel_err")}
+                                    for r in recs],
+                        "seconds": round(time.perf_counter() - t, 1)}
+    return out
 
 
 def run_next(args):

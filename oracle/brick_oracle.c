@@ -144,28 +144,83 @@ static void tap_radius(int npts, const int *offs, int r[3]) {
     }
 }
 
-/* Gather the extended tile (bdim + 2r per axis) of brick b through adj, the way the
+/* The part of a brick's extended tile (bdim + 2r per axis) that a tap list reads: per tile
+ * row (k, j) the column range [lo, hi); lo >= hi when no tap reads the row.  A star reads its
+ * centre brick and the faces it reaches, a cube its whole neighbourhood. */
+typedef struct {
+  int ek, ej, ei;
+  int *lo, *hi;
+} tile_rows;
+
+static tile_rows rows_read(int npts, const int *offs, const int bdim[3], const int r[3]) {
+  tile_rows t;
+  t.ek = bdim[0] + 2 * r[0];
+  t.ej = bdim[1] + 2 * r[1];
+  t.ei = bdim[2] + 2 * r[2];
+  t.lo = (int *)malloc(sizeof(int) * (size_t)t.ek * t.ej);
+  t.hi = (int *)malloc(sizeof(int) * (size_t)t.ek * t.ej);
+  for (long q = 0; q < (long)t.ek * t.ej; ++q) {
+    t.lo[q] = t.ei;
+    t.hi[q] = 0;
+  }
+  for (int p = 0; p < npts; ++p) {
+    const int dk = offs[3 * p], dj = offs[3 * p + 1], di = offs[3 * p + 2];
+    for (int k = 0; k < bdim[0]; ++k)
+      for (int j = 0; j < bdim[1]; ++j) {
+        const long q = (long)(k + r[0] + dk) * t.ej + (j + r[1] + dj);
+        if (r[2] + di < t.lo[q]) t.lo[q] = r[2] + di;
+        if (r[2] + di + bdim[2] > t.hi[q]) t.hi[q] = r[2] + di + bdim[2];
+      }
+  }
+  return t;
+}
+
+static void rows_free(tile_rows *t) {
+  free(t->lo);
+  free(t->hi);
+}
+
+/* 1 when the in-brick layout is row-major (element (k,j,i) at (k*bj + j)*bi + i): brick rows are
+ * then contiguous and copy as one run. */
+static int layout_row_major(const int bdim[3], const long *ot) {
+  const long bs = (long)bdim[0] * bdim[1] * bdim[2];
+  for (long p = 0; p < bs; ++p)
+    if (ot[p] != p) return 0;
+  return 1;
+}
+
+/* Gather the rows of brick b's extended tile that the taps read, through adj, the way the
  * accessor resolves an out-of-brick index: neighbour slot from the sign of the overflow
- * (brick.h:232-245), element from the in-brick remainder. */
-#define DEFINE_GATHER(NAME, T)                                                                \
-  static void NAME(const unsigned *adj, const T *in, long step, long off, unsigned b,        \
-                   const int bdim[3], const int r[3], const long *ot, T *tile) {             \
-    const int ek = bdim[0] + 2 * r[0], ej = bdim[1] + 2 * r[1], ei = bdim[2] + 2 * r[2];     \
-    for (int k = 0; k < ek; ++k) {                                                           \
-      int kk = k - r[0], qk = kk < 0 ? -1 : (kk >= bdim[0] ? 1 : 0);                         \
-      int lk = kk - qk * bdim[0];                                                            \
-      for (int j = 0; j < ej; ++j) {                                                         \
-        int jj = j - r[1], qj = jj < 0 ? -1 : (jj >= bdim[1] ? 1 : 0);                       \
-        int lj = jj - qj * bdim[1];                                                          \
-        for (int i = 0; i < ei; ++i) {                                                       \
-          int ii = i - r[2], qi = ii < 0 ? -1 : (ii >= bdim[2] ? 1 : 0);                     \
-          int li = ii - qi * bdim[2];                                                        \
-          unsigned nb = adj[(size_t)b * 27 + (qk + 1) * 9 + (qj + 1) * 3 + (qi + 1)];        \
-          tile[((long)k * ej + j) * ei + i] =                                                \
-              in[(size_t)nb * step + off + ot[((long)lk * bdim[1] + lj) * bdim[2] + li]];    \
-        }                                                                                    \
-      }                                                                                      \
-    }                                                                                        \
+ * (brick.h:232-245), element from the in-brick remainder.  A tile row spans up to three
+ * bricks along i (the i-lo neighbour, the brick itself, the i-hi neighbour). */
+#define DEFINE_GATHER(NAME, T)                                                                    \
+  static void NAME(const unsigned *adj, const T *in, long step, long off, unsigned b,            \
+                   const int bdim[3], const int r[3], const long *ot, int rm, const tile_rows *tr, \
+                   T *tile) {                                                                    \
+    const int ej = tr->ej, ei = tr->ei, bi = bdim[2];                                            \
+    for (int k = 0; k < tr->ek; ++k) {                                                           \
+      const int kk = k - r[0], qk = kk < 0 ? -1 : (kk >= bdim[0] ? 1 : 0);                       \
+      const int lk = kk - qk * bdim[0];                                                          \
+      for (int j = 0; j < ej; ++j) {                                                             \
+        const int lo = tr->lo[(long)k * ej + j], hi = tr->hi[(long)k * ej + j];                  \
+        if (lo >= hi) continue;                                                                  \
+        const int jj = j - r[1], qj = jj < 0 ? -1 : (jj >= bdim[1] ? 1 : 0);                     \
+        const int lj = jj - qj * bdim[1];                                                        \
+        T *trow = tile + ((long)k * ej + j) * ei;                                                \
+        for (int qi = -1; qi <= 1; ++qi) {                                                       \
+          const int s0 = qi < 0 ? 0 : (qi == 0 ? r[2] : r[2] + bi);                              \
+          const int s1 = qi < 0 ? r[2] : (qi == 0 ? r[2] + bi : ei);                             \
+          const int a = s0 > lo ? s0 : lo, e = s1 < hi ? s1 : hi;                                \
+          if (a >= e) continue;                                                                  \
+          const unsigned nb = adj[(size_t)b * 27 + (qk + 1) * 9 + (qj + 1) * 3 + (qi + 1)];      \
+          const T *src = in + (size_t)nb * step + off;                                           \
+          const long row = ((long)lk * bdim[1] + lj) * bi + (a - r[2] - qi * bi);                \
+          if (rm) memcpy(trow + a, src + row, sizeof(T) * (size_t)(e - a));                      \
+          else                                                                                   \
+            for (int i = a; i < e; ++i) trow[i] = src[ot[row + (i - a)]];                        \
+        }                                                                                        \
+      }                                                                                          \
+    }                                                                                            \
   }
 
 DEFINE_GATHER(gather_f64, double)
@@ -176,6 +231,64 @@ static inline double op_apply(double x, int op) {
   if (op == 2) return x > 0 ? x : -x;     /* partial > 0 ? partial : -partial */
   return x;
 }
+
+/* acc(k,j,i) = sum_t coeff[t] * tile(k+r+dk, j+r+dj, i+r+di), every point summing its taps left
+ * to right.  Any brick dims: taps outermost, over whole brick rows. */
+#define DEFINE_TAPS(NAME, T)                                                                      \
+  static void NAME(const T *restrict tile, int ej, int ei, const int r[3], const int bdim[3],    \
+                   int npts, const int *offs, const double *coeff, T *restrict acc) {           \
+    const int bk = bdim[0], bj = bdim[1], bi = bdim[2];                                          \
+    for (int t = 0; t < npts; ++t) {                                                             \
+      const T c = (T)coeff[t];                                                                   \
+      const int dk = offs[3 * t], dj = offs[3 * t + 1], di = offs[3 * t + 2];                    \
+      for (int k = 0; k < bk; ++k)                                                               \
+        for (int j = 0; j < bj; ++j) {                                                           \
+          const T *src = tile + ((long)(k + r[0] + dk) * ej + (j + r[1] + dj)) * ei + r[2] + di; \
+          T *dst = acc + ((long)k * bj + j) * bi;                                                \
+          if (t == 0)                                                                            \
+            for (int i = 0; i < bi; ++i) dst[i] = c * src[i];                                    \
+          else                                                                                   \
+            for (int i = 0; i < bi; ++i) dst[i] = dst[i] + c * src[i];                           \
+        }                                                                                        \
+    }                                                                                            \
+  }
+
+/* 8^3 bricks: rows outermost, the row's eight sums held in registers across the taps (tap t of
+ * the row at tile offset toff[t] from the row's centre); the same operations per point in the
+ * same order as above. */
+#define DEFINE_TAPS_888(NAME, T)                                                                  \
+  static void NAME(const T *restrict tile, int ej, int ei, const int r[3], int npts,             \
+                   const long *toff, const T *cf, T *restrict acc) {                            \
+    for (int k = 0; k < 8; ++k)                                                                  \
+      for (int j = 0; j < 8; ++j) {                                                              \
+        const T *base = tile + ((long)(k + r[0]) * ej + (j + r[1])) * ei + r[2];                 \
+        T a[8];                                                                                  \
+        const T *s0 = base + toff[0];                                                            \
+        for (int i = 0; i < 8; ++i) a[i] = cf[0] * s0[i];                                        \
+        for (int t = 1; t < npts; ++t) {                                                         \
+          const T c = cf[t];                                                                     \
+          const T *s = base + toff[t];                                                           \
+          for (int i = 0; i < 8; ++i) a[i] = a[i] + c * s[i];                                    \
+        }                                                                                        \
+        memcpy(acc + (k * 8 + j) * 8, a, sizeof(a));                                             \
+      }                                                                                          \
+  }
+
+DEFINE_TAPS(taps_f64, double)
+DEFINE_TAPS(taps_f32, float)
+DEFINE_TAPS_888(taps_f64_888, double)
+DEFINE_TAPS_888(taps_f32_888, float)
+
+/* tile offsets of the taps from a row's centre element, for the 8^3 path */
+static long *tap_offsets(int npts, const int *offs, int ej, int ei) {
+  long *t = (long *)malloc(sizeof(long) * (size_t)(npts > 0 ? npts : 1));
+  for (int p = 0; p < npts; ++p) t[p] = ((long)offs[3 * p] * ej + offs[3 * p + 1]) * ei + offs[3 * p + 2];
+  return t;
+}
+
+#define BK_ORC_MAX_TAPS 1024
+
+static int is_888(const int bdim[3]) { return bdim[0] == 8 && bdim[1] == 8 && bdim[2] == 8; }
 
 void orc_brick_sweep(const unsigned *adj, const double *in, long in_step, long in_off,
                      double *out, long out_step, long out_off,
@@ -193,41 +306,36 @@ void orc_brick_sweep_ops(const unsigned *adj, const double *in, long in_step, lo
                          int npts, const int *offs, const double *coeff, int pre, int post, int nthreads) {
   int r[3];
   tap_radius(npts, offs, r);
-  const int ek = bdim[0] + 2 * r[0], ej = bdim[1] + 2 * r[1], ei = bdim[2] + 2 * r[2];
+  tile_rows tr = rows_read(npts, offs, bdim, r);
   const long bs = (long)bdim[0] * bdim[1] * bdim[2];
   long *ot = offset_table(bdim, fold);
+  const int rm = layout_row_major(bdim, ot), b8 = is_888(bdim);
+  long *toff = tap_offsets(npts, offs, tr.ej, tr.ei);
   if (nthreads <= 0) nthreads = orc_max_threads();
 #pragma omp parallel num_threads(nthreads)
   {
-    double *tile = (double *)malloc(sizeof(double) * (size_t)ek * ej * ei);
+    double *tile = (double *)malloc(sizeof(double) * (size_t)tr.ek * tr.ej * tr.ei);
     double *acc = (double *)malloc(sizeof(double) * (size_t)bs);
 #pragma omp for schedule(static)
     for (long n = 0; n < nlist; ++n) {
       unsigned b = blist[n];
-      gather_f64(adj, in, in_step, in_off, b, bdim, r, ot, tile);
+      gather_f64(adj, in, in_step, in_off, b, bdim, r, ot, rm, &tr, tile);
       if (pre)
-        for (long e = 0; e < (long)ek * ej * ei; ++e) tile[e] = op_apply(tile[e], pre);
-      /* taps outermost, points inner: every point still sums its taps left to right */
-      for (int t = 0; t < npts; ++t) {
-        const double c = coeff[t];
-        const int dk = offs[3 * t], dj = offs[3 * t + 1], di = offs[3 * t + 2];
-        for (int k = 0; k < bdim[0]; ++k)
-          for (int j = 0; j < bdim[1]; ++j) {
-            const double *src = tile + ((long)(k + r[0] + dk) * ej + (j + r[1] + dj)) * ei + r[2] + di;
-            double *dst = acc + ((long)k * bdim[1] + j) * bdim[2];
-            if (t == 0)
-              for (int i = 0; i < bdim[2]; ++i) dst[i] = c * src[i];
-            else
-              for (int i = 0; i < bdim[2]; ++i) dst[i] = dst[i] + c * src[i];
-          }
-      }
+        for (long q = 0; q < (long)tr.ek * tr.ej; ++q)
+          for (int i = tr.lo[q]; i < tr.hi[q]; ++i) tile[q * tr.ei + i] = op_apply(tile[q * tr.ei + i], pre);
+      if (b8) taps_f64_888(tile, tr.ej, tr.ei, r, npts, toff, coeff, acc);
+      else taps_f64(tile, tr.ej, tr.ei, r, bdim, npts, offs, coeff, acc);
       double *ob = out + (size_t)b * out_step + out_off;
-      for (long p = 0; p < bs; ++p) ob[ot[p]] = op_apply(acc[p], post);
+      if (rm && !post) memcpy(ob, acc, sizeof(double) * (size_t)bs);
+      else
+        for (long p = 0; p < bs; ++p) ob[ot[p]] = op_apply(acc[p], post);
     }
     free(tile);
     free(acc);
   }
   free(ot);
+  free(toff);
+  rows_free(&tr);
 }
 
 void orc_brick_sweep_f32(const unsigned *adj, const float *in, long in_step, long in_off,
@@ -237,31 +345,24 @@ void orc_brick_sweep_f32(const unsigned *adj, const float *in, long in_step, lon
                          int npts, const int *offs, const double *coeff, int nthreads) {
   int r[3];
   tap_radius(npts, offs, r);
-  const int ek = bdim[0] + 2 * r[0], ej = bdim[1] + 2 * r[1], ei = bdim[2] + 2 * r[2];
+  tile_rows tr = rows_read(npts, offs, bdim, r);
   const long bs = (long)bdim[0] * bdim[1] * bdim[2];
   long *ot = offset_table(bdim, fold);
+  const int rm = layout_row_major(bdim, ot), b8 = is_888(bdim);
+  long *toff = tap_offsets(npts, offs, tr.ej, tr.ei);
+  float cf[BK_ORC_MAX_TAPS];
+  for (int t = 0; t < npts && t < BK_ORC_MAX_TAPS; ++t) cf[t] = (float)coeff[t];
   if (nthreads <= 0) nthreads = orc_max_threads();
 #pragma omp parallel num_threads(nthreads)
   {
-    float *tile = (float *)malloc(sizeof(float) * (size_t)ek * ej * ei);
+    float *tile = (float *)malloc(sizeof(float) * (size_t)tr.ek * tr.ej * tr.ei);
     float *acc = (float *)malloc(sizeof(float) * (size_t)bs);
 #pragma omp for schedule(static)
     for (long n = 0; n < nlist; ++n) {
       unsigned b = blist[n];
-      gather_f32(adj, in, in_step, in_off, b, bdim, r, ot, tile);
-      for (int t = 0; t < npts; ++t) {
-        const float c = (float)coeff[t];
-        const int dk = offs[3 * t], dj = offs[3 * t + 1], di = offs[3 * t + 2];
-        for (int k = 0; k < bdim[0]; ++k)
-          for (int j = 0; j < bdim[1]; ++j) {
-            const float *src = tile + ((long)(k + r[0] + dk) * ej + (j + r[1] + dj)) * ei + r[2] + di;
-            float *dst = acc + ((long)k * bdim[1] + j) * bdim[2];
-            if (t == 0)
-              for (int i = 0; i < bdim[2]; ++i) dst[i] = c * src[i];
-            else
-              for (int i = 0; i < bdim[2]; ++i) dst[i] = dst[i] + c * src[i];
-          }
-      }
+      gather_f32(adj, in, in_step, in_off, b, bdim, r, ot, rm, &tr, tile);
+      if (b8 && npts <= BK_ORC_MAX_TAPS) taps_f32_888(tile, tr.ej, tr.ei, r, npts, toff, cf, acc);
+      else taps_f32(tile, tr.ej, tr.ei, r, bdim, npts, offs, coeff, acc);
       float *ob = out + (size_t)b * out_step + out_off;
       for (long p = 0; p < bs; ++p) ob[ot[p]] = acc[p];
     }
@@ -269,6 +370,8 @@ void orc_brick_sweep_f32(const unsigned *adj, const float *in, long in_step, lon
     free(acc);
   }
   free(ot);
+  free(toff);
+  rows_free(&tr);
 }
 
 void orc_array_sweep(const double *in, double *out, const long dims[3],

@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+TIMED_PATH = os.path.join(HERE, "liboracle_timed.so")
 REF_PATH = os.path.join(HERE, "_ref", "libbrickref.so")
 
 _u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
@@ -43,49 +44,64 @@ def reference_tree() -> Optional[str]:
 
 def build(force: bool = False) -> None:
     """Compile liboracle.so (and _ref/ when the reference tree is present)."""
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    if force or not os.path.exists(LIB_PATH) or not os.path.exists(TIMED_PATH):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all", "timed"])
     tree = reference_tree()
     if tree and (force or not os.path.exists(REF_PATH)):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={tree}"])
 
 
 _lib = None
+_timed = None
 _ref = None
 
 
 def lib():
+    """The parity build (-ffp-contract=off): every check runs on this one."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
-        L = C.CDLL(LIB_PATH)
-        L.orc_fill_uniform.argtypes = [_f64p, C.c_long, C.c_uint64, C.c_double, C.c_double]
-        L.orc_fill_sines.argtypes = [_f64p, _l3, _l3, _l3, C.c_int, C.c_uint64, C.c_double]
-        L.orc_init_grid.argtypes = [_u32p, _u32p, C.c_long, C.c_long, C.c_long]
-        L.orc_brick_offset.argtypes = [_i3, _i3, C.c_int, C.c_int, C.c_int]
-        L.orc_brick_offset.restype = C.c_long
-        L.orc_copy_brick.argtypes = [C.c_int, _l3, _l3, _l3, _f64p, _u32p, _f64p, C.c_long, C.c_long, _i3, _i3]
-        L.orc_brick_sweep.argtypes = [_u32p, _f64p, C.c_long, C.c_long, _f64p, C.c_long, C.c_long,
-                                      _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int]
-        L.orc_brick_sweep_f32.argtypes = [_u32p, _f32p, C.c_long, C.c_long, _f32p, C.c_long, C.c_long,
-                                          _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int]
-        L.orc_array_sweep.argtypes = [_f64p, _f64p, _l3, _l3, _l3, C.c_int, _i32p, _f64p, C.c_int]
-        L.orc_brick_sweep_ops.argtypes = [_u32p, _f64p, C.c_long, C.c_long, _f64p, C.c_long, C.c_long,
-                                          _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int, C.c_int,
-                                          C.c_int]
-        L.orc_array_sweep_ops.argtypes = [_f64p, _f64p, _l3, _l3, _l3, C.c_int, _i32p, _f64p, C.c_int, C.c_int,
-                                          C.c_int]
-        L.orc_array_periodic_fill.argtypes = [_f64p, _l3, _l3, _l3, _l3]
-        L.orc_periodic_plan.argtypes = [_u32p, _l3, _l3, C.c_void_p]
-        L.orc_periodic_plan.restype = C.c_long
-        L.orc_apply_plan.argtypes = [_f64p, C.c_long, C.c_long, C.c_long, _u32p, C.c_long]
-        L.orc_compare_brick.argtypes = [_l3, _l3, _l3, _f64p, _u32p, _f64p, C.c_long, C.c_long,
-                                        _i3, _i3, C.c_double, _f64p]
-        L.orc_compare_brick.restype = C.c_long
-        L.orc_max_threads.restype = C.c_int
-        _lib = L
+        _lib = _load(LIB_PATH)
     return _lib
+
+
+def timed_lib():
+    """The same source built as the reference builds its CPU path (-O2, multiply-adds fused):
+    only the timed CPU baseline runs on it."""
+    global _timed
+    if _timed is None:
+        _timed = _load(TIMED_PATH)
+    return _timed
+
+
+def _load(path):
+    if not os.path.exists(path):
+        build()
+    L = C.CDLL(path)
+    L.orc_fill_uniform.argtypes = [_f64p, C.c_long, C.c_uint64, C.c_double, C.c_double]
+    L.orc_fill_sines.argtypes = [_f64p, _l3, _l3, _l3, C.c_int, C.c_uint64, C.c_double]
+    L.orc_init_grid.argtypes = [_u32p, _u32p, C.c_long, C.c_long, C.c_long]
+    L.orc_brick_offset.argtypes = [_i3, _i3, C.c_int, C.c_int, C.c_int]
+    L.orc_brick_offset.restype = C.c_long
+    L.orc_copy_brick.argtypes = [C.c_int, _l3, _l3, _l3, _f64p, _u32p, _f64p, C.c_long, C.c_long, _i3, _i3]
+    L.orc_brick_sweep.argtypes = [_u32p, _f64p, C.c_long, C.c_long, _f64p, C.c_long, C.c_long,
+                                  _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int]
+    L.orc_brick_sweep_f32.argtypes = [_u32p, _f32p, C.c_long, C.c_long, _f32p, C.c_long, C.c_long,
+                                      _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int]
+    L.orc_array_sweep.argtypes = [_f64p, _f64p, _l3, _l3, _l3, C.c_int, _i32p, _f64p, C.c_int]
+    L.orc_brick_sweep_ops.argtypes = [_u32p, _f64p, C.c_long, C.c_long, _f64p, C.c_long, C.c_long,
+                                      _u32p, C.c_long, _i3, _i3, C.c_int, _i32p, _f64p, C.c_int, C.c_int,
+                                      C.c_int]
+    L.orc_array_sweep_ops.argtypes = [_f64p, _f64p, _l3, _l3, _l3, C.c_int, _i32p, _f64p, C.c_int, C.c_int,
+                                      C.c_int]
+    L.orc_array_periodic_fill.argtypes = [_f64p, _l3, _l3, _l3, _l3]
+    L.orc_periodic_plan.argtypes = [_u32p, _l3, _l3, C.c_void_p]
+    L.orc_periodic_plan.restype = C.c_long
+    L.orc_apply_plan.argtypes = [_f64p, C.c_long, C.c_long, C.c_long, _u32p, C.c_long]
+    L.orc_compare_brick.argtypes = [_l3, _l3, _l3, _f64p, _u32p, _f64p, C.c_long, C.c_long,
+                                    _i3, _i3, C.c_double, _f64p]
+    L.orc_compare_brick.restype = C.c_long
+    L.orc_max_threads.restype = C.c_int
+    return L
 
 
 def ref() -> Optional[C.CDLL]:
@@ -140,15 +156,18 @@ def copy_brick(to_brick: bool, dim, pad, ghost, arr: np.ndarray, grid: np.ndarra
 
 
 def brick_sweep(adj, inp, in_step, in_off, out, out_step, out_off, blist, bdim, fold,
-                offs: np.ndarray, coeff: np.ndarray, nthreads: int = 0, pre: int = 0, post: int = 0) -> None:
+                offs: np.ndarray, coeff: np.ndarray, nthreads: int = 0, pre: int = 0, post: int = 0,
+                timed: bool = False) -> None:
+    """The brick sweep on the parity build, or with `timed` on the timed build (CPU baseline)."""
     offs = np.ascontiguousarray(offs, dtype=np.int32).reshape(-1)
     coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+    L = timed_lib() if timed else lib()
     if pre or post:
-        lib().orc_brick_sweep_ops(adj, inp.reshape(-1), in_step, in_off, out.reshape(-1), out_step, out_off,
+        L.orc_brick_sweep_ops(adj, inp.reshape(-1), in_step, in_off, out.reshape(-1), out_step, out_off,
                                   blist, len(blist), _i3(*bdim), _i3(*fold), len(coeff), offs, coeff, pre, post,
                                   nthreads)
         return
-    fn = lib().orc_brick_sweep if inp.dtype == np.float64 else lib().orc_brick_sweep_f32
+    fn = L.orc_brick_sweep if inp.dtype == np.float64 else L.orc_brick_sweep_f32
     fn(adj, inp.reshape(-1), in_step, in_off, out.reshape(-1), out_step, out_off,
        blist, len(blist), _i3(*bdim), _i3(*fold), len(coeff), offs, coeff, nthreads)
 
