@@ -409,26 +409,31 @@ def run_ours(args):
 
 
 def fp_instructions_per_point(st, acc, dtype=None) -> float:
-    """Floating-point instructions per point of the kernel that runs `st` (native arithmetic on
-    8x8x8 row-major bricks): a multiply-add per tap, except mirror-symmetric cubes, which the
-    pipelined kernel evaluates from pair sums (sweep2_kernel.cuh, FAM_CUBESYM); for FP64
-    storage it streams columns along i (sym_cube_istream: per column the class sums of both
-    rows of a lane, one multiply-add per class and i distance, 2R adds for the i taps; fewer
-    classes when the coefficients are also symmetric under k <-> j), counted in long runs."""
+    """Floating-point operations per point of the kernel that runs `st` on 8x8x8 row-major bricks:
+    a multiply-add per tap, except mirror-symmetric cubes, which stream class sums along i
+    (sweep2_kernel.cuh sym_cube_istream, FP64, and sym_cube_istream4, FP32 / BF16 storage): per
+    point (R+1)R additions for the j pair sums H, R(R+1) for the k pair sums Q, R(R+1)/2 more
+    when the coefficients are also symmetric under k <-> j, one operation per class and i
+    distance for the W sums, 2R for the i taps (37 for the 125-point cube with k <-> j symmetry,
+    43 without).  Compensated FP32 runs each W sum as Dot2 (ten operations per term after the
+    first) and the output sum Neumaier-compensated.  Float-float and the other accumulation
+    modes take a multiply-add per tap."""
     from bricklib_gb300 import _abi
     taps = [tuple(t) for t in st.taps]
     r = st.radius
     cube = len(taps) == (2 * r + 1) ** 3 and len(set(taps)) == len(taps) and r in (1, 2)
-    if not cube or acc != _abi.BK_ACC_NATIVE:
+    comp = acc == _abi.BK_ACC_COMPENSATED and dtype in (_abi.BK_F32, _abi.BK_BF16)
+    if not cube or not (acc == _abi.BK_ACC_NATIVE or comp):
         return float(len(taps))
     c = {t: v for t, v in zip(taps, st.coeff)}
     if any(c[t] != c[tuple(abs(a) for a in t)] for t in taps):
         return float(len(taps))
-    ij = all(c[(k, j, i)] == c[(k, i, j)] for (k, j, i) in taps)
-    if dtype == _abi.BK_F64:
-        kj = all(c[(k, j, i)] == c[(j, k, i)] for (k, j, i) in taps)
-        return {(1, False): 14.0, (1, True): 13.0, (2, False): 43.0, (2, True): 37.0}[(r, kj)]
-    return {(1, False): 18.25, (1, True): 16.5, (2, False): 69.0, (2, True): 58.5}[(r, ij)]
+    kj = all(c[(k, j, i)] == c[(j, k, i)] for (k, j, i) in taps)
+    ncls = (r + 1) * (r + 2) // 2 if kj else (r + 1) ** 2
+    sums = (r + 1) * r + r * (r + 1) + (r * (r + 1) // 2 if kj else 0)
+    if comp:
+        return float(sums + (r + 1) * (2 + 10 * (ncls - 1)) + 10 * r + 2)
+    return float(sums + (r + 1) * ncls + 2 * r)
 
 
 def cpu_info(threads: int) -> dict:

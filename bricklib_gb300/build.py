@@ -87,6 +87,32 @@ def build_cpp_driver(verbose: bool = False) -> str:
     return exe
 
 
+def build_lowered_program(src: str, exe: str, verbose: bool = False) -> str:
+    """A C++ brick program with brick("x.py", ...) statements: lowered by
+    bricklib_gb300.dsl.vecscatter (as the reference's build runs its code generator first),
+    then compiled and linked against the library."""
+    from .dsl import vecscatter
+    lib = build()
+    with open(src) as f:
+        text, report = vecscatter.lower_source(f.read(), os.path.abspath(src))
+    missed = [r for r in report if not r["lowered"]]
+    if missed:
+        raise RuntimeError(f"{src}: brick(...) statements not lowered: {missed}")
+    lowered = exe + ".lowered.cpp"
+    with open(lowered, "w") as f:
+        f.write(text)
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = ["g++", "-O2", "-fopenmp", "-std=c++17", "-I", INCLUDE, "-I", os.path.join(cuda, "include"),
+           "-I", os.path.dirname(os.path.abspath(src)), lowered, "-o", exe, "-L", os.path.dirname(lib),
+           "-lbrick_gb300", "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.dirname(lib)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed on the lowered {src}:\n{r.stdout}\n{r.stderr}")
+    return exe
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
     print(build_cpp_driver(verbose="-v" in sys.argv))

@@ -179,6 +179,12 @@ int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndo
   BK_B2(BK_, BJ_, BI_, 1, FAM_STAR) BK_B2(BK_, BJ_, BI_, 2, FAM_STAR) BK_B2(BK_, BJ_, BI_, 4, FAM_STAR) \
   BK_B2(BK_, BJ_, BI_, 1, FAM_CUBE) BK_B2(BK_, BJ_, BI_, 2, FAM_CUBE)
     if (p.shape == 0) {
+      if constexpr (sizeof(T) <= 4 && (ACC == ACCM_NATIVE || ACC == ACCM_COMP)) {
+        // mirror-symmetric cubes on 4-byte storage: the class sums of the plain sweep's stream, one
+        // brick at a time (the same bits as the plain sweep of the same bricks)
+        if (p.sym && p.fam == FAM_CUBE && p.r == 1) return launch_sweep2<T, 8, 8, 8, 1, FAM_CUBESYM, ACC, true, true>(a, tp, s, grid_cap);
+        if (p.sym && p.fam == FAM_CUBE && p.r == 2) return launch_sweep2<T, 8, 8, 8, 2, FAM_CUBESYM, ACC, true, true>(a, tp, s, grid_cap);
+      }
       if constexpr (ACC == ACCM_NATIVE) {  // mirror-symmetric cubes: the pair-sum variant
         if (p.symij && p.fam == FAM_CUBE && p.r == 1) return launch_sweep2<T, 8, 8, 8, 1, FAM_CUBESYM_IJ, ACC, true>(a, tp, s, grid_cap);
         if (p.symij && p.fam == FAM_CUBE && p.r == 2) return launch_sweep2<T, 8, 8, 8, 2, FAM_CUBESYM_IJ, ACC, true>(a, tp, s, grid_cap);

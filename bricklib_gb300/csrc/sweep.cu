@@ -119,6 +119,7 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
             tp->c[q] = tp->c[m];
             tp->cf[q] = tp->cf[m];
             tp->cl[q] = tp->cl[m];
+            tp->sp[(ak * (r + 1) + aj) * (r + 1) + ai] = make_float2(tp->cf[m], tp->cf[m]);
           }
       bool ij = true;
       for (int ak = 0; ak <= r; ++ak)
@@ -177,11 +178,13 @@ static int plan_sweep(const bk_field *in, const bk_field *out, const bk_stencil 
     if (plan->fam == FAM_CUBE && plan->shape == 0 && !plan->out_pair) plan->v2 = false;
     // star stencils on 8x8x8 row-major bricks: the TMA-fed kernel, unless a kernel is forced
     plan->tma = tma_eligible(*plan, in) && !getenv("BK_SWEEP_ONESHOT") && !getenv("BK_SWEEP_PIPELINED");
-    // FP64 mirror-symmetric cubes: the pipelined kernel streams columns along i (BK_SWEEP_ISTREAM=0:
-    // one brick at a time)
+    // mirror-symmetric cubes: the pipelined kernel streams class sums along i -- FP64 in native
+    // arithmetic, FP32 / BF16 in native or compensated FP32 (BK_SWEEP_ISTREAM=0: one brick at a
+    // time on column pairs)
     const char *ist = getenv("BK_SWEEP_ISTREAM");
-    plan->istream = plan->v2 && plan->sym && plan->shape == 0 && in->dtype == BK_F64 && plan->acc == ACCM_NATIVE &&
-                    !(ist && !strcmp(ist, "0"));
+    plan->istream = plan->v2 && plan->sym && plan->shape == 0 && !(ist && !strcmp(ist, "0")) &&
+                    (in->dtype == BK_F64 ? plan->acc == ACCM_NATIVE
+                                         : (plan->acc == ACCM_NATIVE || plan->acc == ACCM_COMP));
   }
   *Lout = L;
   return BK_OK;

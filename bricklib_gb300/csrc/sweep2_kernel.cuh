@@ -95,7 +95,9 @@ __host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, in
 #endif
 constexpr int PAIR_NB = BK_PAIR_NB;
 
-template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
+// IST: the class-sum stream of the mirror-symmetric cubes (sym_cube_istream for FP64,
+// sym_cube_istream4 for 4- and 2-byte storage), one warp per 8x8x8 brick.
+template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool IST = false>
 struct Sweep2Cfg {
   static constexpr int ES = (int)sizeof(T);
   static constexpr int VB = cmin(16, BI * ES);  // bytes per copy
@@ -109,7 +111,13 @@ struct Sweep2Cfg {
   // reads fall in disjoint banks.
   static constexpr bool PERM = ES == 8 && BI == 8;
   static constexpr int NEED = BI + 2 * RP;
-  static constexpr int EI = PERM ? (NEED % 8 <= 4 ? NEED - NEED % 8 + 4 : NEED - NEED % 8 + 12)
+  // the class-sum stream of 4- / 2-byte storage reads 4 columns of 32 rows at once (16 / 8
+  // bytes per lane): rows of 20 FP32 elements put the 8 rows of a quarter warp in distinct
+  // 4-bank groups (16-byte reads, conflict free); BF16 rows of 24 (two-way within a half warp,
+  // which reads half the bytes of the FP32 case)
+  static constexpr bool CS4 = IST && ES <= 4;
+  static constexpr int EI = CS4 ? (ES == 4 ? 20 : 24)
+                          : PERM ? (NEED % 8 <= 4 ? NEED - NEED % 8 + 4 : NEED - NEED % 8 + 12)
                                  : conflict_free_row(NEED, BI, ES, VE);
   static constexpr int TILE = EK * EJ * EI;  // elements per brick tile
   static constexpr int TILE_BYTES = (TILE * ES + 15) / 16 * 16;
@@ -120,7 +128,8 @@ struct Sweep2Cfg {
   // cube125 191 / 156; BF16 cube27 412 / 302, cube125 235 / 139).
   static constexpr bool PAIR = BK == 8 && BJ == 8 && BI == 8 && ACC == ACCM_NATIVE &&
                                (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ || (FAM == FAM_CUBE && R == 1 && ES <= 4));
-  static constexpr int TPB = PAIR ? BJ * BI / 2 : BJ * BI;
+  static constexpr bool WARP1 = PAIR || CS4;  // one warp per brick
+  static constexpr int TPB = WARP1 ? BJ * BI / 2 : BJ * BI;
   // vectors of the neighbourhood (per brick)
   static constexpr int NV_CENTRE = BK * BJ * (BI / VE);
   static constexpr int NV_KF = R * BJ * (BI / VE);   // one k face
@@ -134,7 +143,7 @@ struct Sweep2Cfg {
   static constexpr int FTILE_BYTES = 0;
   // bricks per CTA: as many as fit 128 threads and a ~100 KB shared-memory budget
   static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 36 * 4;
-  static constexpr int NB = PAIR ? PAIR_NB : cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
+  static constexpr int NB = CS4 ? 1 : PAIR ? PAIR_NB : cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
   static constexpr int NT = TPB * NB;
   static constexpr int SMEM = NB * PER_BRICK;
 };
@@ -483,6 +492,232 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Mirror-symmetric cubes on 4- and 2-byte storage in FP32 arithmetic, streamed along i: the
+// class sums of sym_cube_istream, four tile columns per step.  A lane owns rows (k0, j) and
+// (k0 + 1, j) of the brick as in the FP64 stream, and reads each of the 2R + 1 rows j - R ..
+// j + R of the 2R + 2 planes it needs as one 16-byte (FP32) / 8-byte (BF16) load of four
+// columns; all arithmetic runs on column pairs (i, i + 1) in packed FP32 (FADD2 / FFMA2):
+//   H_b  = x(j - b) + x(j + b)                        per plane, shared by both rows
+//   Q(c, b) = H_b(k - c) + H_b(k + c)                 per row; Q(c, b) += Q(b, c) under k <-> j
+//   W_a  = sum over classes of coef(c, b, a) Q(c, b)  a = 0..R
+//   out(i) = W_0(i) + sum over a of (W_a(i - a) + W_a(i + a))
+// (per point 37 FP32 operations for the 125-point cube with k <-> j symmetry, in 19 packed
+// instructions).  W of the columns already computed carry from one brick of a stream to the
+// next (two 4-column groups), so a continued brick reads only its own eight columns.  Each W
+// depends on one column only and the output sums run in a fixed order, so a brick's outputs
+// are the same bits however it was reached.
+// Compensated accumulation (ACCM_COMP): every W sum runs as Dot2 (the error of each product by
+// FMA, of each addition by TwoSum, summed apart and added at the end) and the output sum is
+// Neumaier-compensated with the W errors folded in; the remaining error is that of the
+// additions in H and Q, about the error of the one-column compensated code.
+
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// four consecutive tile elements as two column pairs
+__device__ __forceinline__ void ld_quad(const float *p, float2 &a, float2 &b) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  a = make_float2(v.x, v.y);
+  b = make_float2(v.z, v.w);
+}
+__device__ __forceinline__ void ld_quad(const __nv_bfloat16 *p, float2 &a, float2 &b) {
+  const uint2 u = *reinterpret_cast<const uint2 *>(p);
+  a = make_float2(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u));
+  b = make_float2(__uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u));
+}
+__device__ __forceinline__ void st_elem(float *p, float v) { *p = v; }
+__device__ __forceinline__ void st_elem(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+// four parked outputs (tile) -> global memory: one 16-byte (FP32) / 8-byte (BF16) store
+__device__ __forceinline__ void st_quad(float *g, const float *t) {
+  __stcs(reinterpret_cast<float4 *>(g), *reinterpret_cast<const float4 *>(t));
+}
+__device__ __forceinline__ void st_quad(__nv_bfloat16 *g, const __nv_bfloat16 *t) {
+  __stcs(reinterpret_cast<uint2 *>(g), *reinterpret_cast<const uint2 *>(t));
+}
+
+// W of the current and previous 4-column groups of a stream, per row o, a = 0..R and column
+// pair; with the Dot2 error terms of each W under compensated accumulation.
+template <int R, bool COMP>
+struct CsWin {
+  float2 p[2][R + 1][2], c[2][R + 1][2];
+  float2 ep[COMP ? 2 : 1][R + 1][2], ec[COMP ? 2 : 1][R + 1][2];
+};
+
+// W_a (and errors) of the four tile columns c0 .. c0 + 3 for both rows of this lane.
+// base: tile element (plane k0, row j, column 0), i.e. brick-local (k0 - R, j - R, -RP).
+template <typename C, typename T, int R, bool KJ, bool COMP>
+__device__ __forceinline__ void cs_group(const T *base, const int c0, const Taps &tp, float2 (&W)[2][R + 1][2],
+                                         float2 (&E)[COMP ? 2 : 1][R + 1][2]) {
+  constexpr int SK = C::EJ * C::EI, SJ = C::EI;
+  float2 Q[2][R + 1][R + 1][2];  // [o][c][b][pair]
+#pragma unroll
+  for (int q = 0; q < 2 * R + 2; ++q) {  // tile plane k0 + q: brick-local plane k0 - R + q
+    float2 v[2 * R + 1][2];
+#pragma unroll
+    for (int rr = 0; rr <= 2 * R; ++rr) ld_quad(base + q * SK + rr * SJ + c0, v[rr][0], v[rr][1]);
+    float2 H[R + 1][2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      H[0][h] = v[R][h];
+#pragma unroll
+      for (int b = 1; b <= R; ++b) H[b][h] = __fadd2_rn(v[R - b][h], v[R + b][h]);
+    }
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      const int dk = q - R - o;  // offset of this plane from row k0 + o
+      if (dk < -R || dk > R) continue;
+      const int c = dk < 0 ? -dk : dk;
+#pragma unroll
+      for (int b = 0; b <= R; ++b)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          Q[o][c][b][h] = dk == -c ? H[b][h] : __fadd2_rn(Q[o][c][b][h], H[b][h]);
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < 2; ++o) {
+    if constexpr (KJ) {
+#pragma unroll
+      for (int c = 1; c <= R; ++c)
+#pragma unroll
+        for (int b = 0; b < c; ++b)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) Q[o][c][b][h] = __fadd2_rn(Q[o][c][b][h], Q[o][b][c][h]);
+    }
+#pragma unroll
+    for (int a = 0; a <= R; ++a)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float2 w = make_float2(0.f, 0.f), e = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c <= R; ++c)
+#pragma unroll
+          for (int b = 0; b <= (KJ ? c : R); ++b) {
+            const float2 cf = tp.sp[(c * (R + 1) + b) * (R + 1) + a];
+            const float2 x = Q[o][c][b][h];
+            if constexpr (!COMP) {
+              w = (c == 0 && b == 0) ? __fmul2_rn(cf, x) : __ffma2_rn(cf, x, w);
+            } else {
+              const float2 pr = __fmul2_rn(cf, x);
+              const float2 pe = __ffma2_rn(cf, x, neg2(pr));  // the product's rounding error, exact
+              if (c == 0 && b == 0) {
+                w = pr;
+                e = pe;
+              } else {  // TwoSum(w, pr): sm + ew == w + pr exactly
+                const float2 sm = __fadd2_rn(w, pr);
+                const float2 bb = __fadd2_rn(sm, neg2(w));
+                const float2 ew = __fadd2_rn(__fadd2_rn(w, neg2(__fadd2_rn(sm, neg2(bb)))), __fadd2_rn(pr, neg2(bb)));
+                e = __fadd2_rn(e, __fadd2_rn(ew, pe));
+                w = sm;
+              }
+            }
+          }
+        W[o][a][h] = w;
+        if constexpr (COMP) E[o][a][h] = e;
+      }
+  }
+}
+
+// W_a (or its error) at column rel of the current group (rel in [-4, 8): previous, current,
+// next group), for row o.
+template <int R, int NO>
+__device__ __forceinline__ float cs_at(const float2 (&P)[NO][R + 1][2], const float2 (&Cc)[NO][R + 1][2],
+                                       const float2 (&N)[NO][R + 1][2], int o, int a, int rel) {
+  const float2 (*g)[R + 1][2] = rel < 0 ? P : rel < 4 ? Cc : N;
+  const int m = (rel + 4) & 3;
+  const float2 v = g[o][a][m >> 1];
+  return (m & 1) ? v.y : v.x;
+}
+
+// Outputs of the current group's four columns for both rows, parked in the tile (park: tile
+// element (plane k0 + R, row j + R) at the group's first column).
+template <typename C, typename T, int R, bool COMP>
+__device__ __forceinline__ void cs_out(T *park, const CsWin<R, COMP> &S, const float2 (&Wn)[2][R + 1][2],
+                                       const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
+  constexpr int SK = C::EJ * C::EI;
+#pragma unroll
+  for (int o = 0; o < 2; ++o)
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      float v;
+      if constexpr (!COMP) {
+        v = cs_at<R, 2>(S.p, S.c, Wn, o, 0, t);
+#pragma unroll
+        for (int a = 1; a <= R; ++a) v += cs_at<R, 2>(S.p, S.c, Wn, o, a, t - a) + cs_at<R, 2>(S.p, S.c, Wn, o, a, t + a);
+      } else {
+        float sm = cs_at<R, 2>(S.p, S.c, Wn, o, 0, t), cm = 0.f;
+        float es = cs_at<R, 2>(S.ep, S.ec, En, o, 0, t);
+#pragma unroll
+        for (int a = 1; a <= R; ++a) {
+          neumaier(sm, cm, cs_at<R, 2>(S.p, S.c, Wn, o, a, t - a));
+          neumaier(sm, cm, cs_at<R, 2>(S.p, S.c, Wn, o, a, t + a));
+          es += cs_at<R, 2>(S.ep, S.ec, En, o, a, t - a) + cs_at<R, 2>(S.ep, S.ec, En, o, a, t + a);
+        }
+        v = sm + (cm + es);
+      }
+      st_elem(park + o * SK + t, v);
+    }
+}
+
+template <int R, bool COMP>
+__device__ __forceinline__ void cs_shift(CsWin<R, COMP> &S, const float2 (&Wn)[2][R + 1][2],
+                                         const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
+#pragma unroll
+  for (int o = 0; o < 2; ++o)
+#pragma unroll
+    for (int a = 0; a <= R; ++a)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        S.p[o][a][h] = S.c[o][a][h];
+        S.c[o][a][h] = Wn[o][a][h];
+        if constexpr (COMP) {
+          S.ep[o][a][h] = S.ec[o][a][h];
+          S.ec[o][a][h] = En[o][a][h];
+        }
+      }
+}
+
+// One brick of the stream: its eight output columns (groups at tile columns RP and RP + 4), the
+// W of groups RP - 4 and RP computed here unless the stream continues (cont), then the brick
+// leaves in whole-warp stores (16 / 8 bytes per lane) when the output brick is aligned for them.
+template <typename C, typename T, int R, bool KJ, bool COMP>
+__device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, const Taps &tp, CsWin<R, COMP> &S,
+                                                  const bool cont) {
+  constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP;
+  static_assert(R == 1 || R == 2, "cube radius");
+  static_assert(RP >= 4 && C::NEED >= RP + 12, "the four column groups of a brick fit the tile row");
+  const int k0 = 2 * (lane >> 3), j = lane & 7;
+  const T *base = rt + k0 * SK + j * SJ;
+  T *park = rt + (k0 + R) * SK + (j + R) * SJ;
+  float2 Wn[2][R + 1][2], En[COMP ? 2 : 1][R + 1][2];
+  if (!cont) {
+    cs_group<C, T, R, KJ, COMP>(base, RP - 4, tp, S.p, S.ep);
+    cs_group<C, T, R, KJ, COMP>(base, RP, tp, S.c, S.ec);
+  }
+  cs_group<C, T, R, KJ, COMP>(base, RP + 4, tp, Wn, En);
+  __syncwarp();  // every lane is past its reads of columns RP .. RP + 7
+  cs_out<C, T, R, COMP>(park + RP, S, Wn, En);
+  cs_shift<R, COMP>(S, Wn, En);
+  cs_group<C, T, R, KJ, COMP>(base, RP + 8, tp, Wn, En);  // the i-hi columns: never parked over
+  cs_out<C, T, R, COMP>(park + RP + 4, S, Wn, En);
+  cs_shift<R, COMP>(S, Wn, En);
+  __syncwarp();  // the parked outputs of every lane are in the tile
+  constexpr int AL = 4 * (int)sizeof(T);
+  if ((reinterpret_cast<uintptr_t>(ob) & (AL - 1)) == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = q * 128 + 4 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
+      st_quad(ob + e, rt + (k + R) * SK + (jj + R) * SJ + RP + i);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int e = q * 32 + lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
+      ob[e] = rt[(k + R) * SK + (jj + R) * SJ + RP + i];
+    }
+  }
+}
+
 // One brick's outputs from its staged tile (the compute of sweep2_kernel): each of the BJ*BI
 // threads (lt) owns one (j, i) column, or, for the column-pair cubes, each of the BJ*BI/2
 // threads a pair of columns.
@@ -748,12 +983,16 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
 // IST: FP64 mirror-symmetric cubes streamed along i (sym_cube_istream): each CTA takes a
 // contiguous share of the list instead of every gridDim.x-th group.
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH, bool IST>
-__global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC>::NT)
+__global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST>::NT)
 sweep2_kernel(const SweepArgs a, const Taps tp) {
-  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
+  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST> C;
   constexpr int TPB = C::TPB, NB = C::NB, EPT = C::EPT;
-  static_assert(!IST || (C::PAIR && C::ES == 8 && NB == 1 && !BATCH && (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ)),
-                "i-streaming is for FP64 mirror-symmetric cubes, one brick per CTA, plain lists");
+  static_assert(!IST || (C::ES == 8 && C::PAIR && NB == 1 && !BATCH && (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ)) ||
+                    (C::ES <= 4 && C::CS4 && NB == 1 && FAM == FAM_CUBESYM && ACC != ACCM_FF),
+                "class-sum streams: FP64 mirror-symmetric cubes on plain lists, or FP32 / BF16 ones (batch mode: "
+                "one brick at a time), one brick per CTA");
+  // 4- / 2-byte storage: a stream along the list in plain mode; brick by brick in batch mode
+  constexpr bool STREAM = IST && !BATCH;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
@@ -775,9 +1014,9 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
   // this CTA's groups: g0, g0 + gstride, ... below gend
-  const long long g0 = IST ? (long long)blockIdx.x * ngroups / gridDim.x : (long long)blockIdx.x;
-  const long long gend = IST ? ((long long)blockIdx.x + 1) * ngroups / gridDim.x : ngroups;
-  const long long gstride = IST ? 1 : (long long)gridDim.x;
+  const long long g0 = STREAM ? (long long)blockIdx.x * ngroups / gridDim.x : (long long)blockIdx.x;
+  const long long gend = STREAM ? ((long long)blockIdx.x + 1) * ngroups / gridDim.x : ngroups;
+  const long long gstride = STREAM ? 1 : (long long)gridDim.x;
 
   // Adjacency of a group: fetched into registers two groups ahead (its global-load latency
   // hides under the current group's compute), stored into one of three nbrs slots.
@@ -882,8 +1121,10 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   __syncthreads();
   issue(0, 0);
 
-  // i-streaming: W of the last 2R columns of the previous brick (sym_cube_istream)
-  double W[IST ? 2 : 1][IST ? R + 1 : 1][IST ? 2 * R + 1 : 1];
+  // i-streaming: W of the last 2R columns of the previous brick (sym_cube_istream), or of the
+  // last two 4-column groups (sym_cube_istream4)
+  double W[IST && C::ES == 8 ? 2 : 1][IST && C::ES == 8 ? R + 1 : 1][IST && C::ES == 8 ? 2 * R + 1 : 1];
+  CsWin<R, ACC == ACCM_COMP> S4;
 
   for (int it = 0; grp < gend; grp += gstride, ++it) {
     const int cur = it & 1, nxt = cur ^ 1;
@@ -908,21 +1149,30 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
       // the stream continues when the previous group (list entry grp - 1, adjacency still in
       // nbrs[nfar]) ran and its centre and i-hi columns of neighbours are this brick's i-lo
       // and centre columns
-      const unsigned *prv = nbrs + nfar * 36;
-      bool same = true;
-      if (lt < 18) {
-        const int s9 = lt < 9 ? lt : lt - 9, sh = lt < 9 ? 0 : 1;
-        const int base = (s9 / 3) * 9 + (s9 % 3) * 3;  // (dk, dj) = (s9 / 3 - 1, s9 % 3 - 1), di = -1
-        same = nbr[base + sh] == prv[base + sh + 1];
+      bool cont = false;
+      if constexpr (STREAM) {
+        const unsigned *prv = nbrs + nfar * 36;
+        bool same = true;
+        if (lt < 18) {
+          const int s9 = lt < 9 ? lt : lt - 9, sh = lt < 9 ? 0 : 1;
+          const int base = (s9 / 3) * 9 + (s9 % 3) * 3;  // (dk, dj) = (s9 / 3 - 1, s9 % 3 - 1), di = -1
+          same = nbr[base + sh] == prv[base + sh + 1];
+        }
+        cont = __all_sync(0xFFFFFFFFu, same) && it > 0 && prv[27] != 0 && active;
       }
-      const bool cont = __all_sync(0xFFFFFFFFu, same) && it > 0 && prv[27] != 0 && active;
       if (active) {
         T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
         const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
         T *ob = out + (size_t)nbr[13] * ostep;
-        double *tile = const_cast<double *>(rt);  // this warp's buffer until the next barrier
-        if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, tp, W, cont);
-        else sym_cube_istream<C, R, false>(tile, ob, lt, tp, W, cont);
+        T *tile = const_cast<T *>(rt);  // this warp's buffer until the next barrier
+        if constexpr (C::ES == 8) {
+          if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, tp, W, cont);
+          else sym_cube_istream<C, R, false>(tile, ob, lt, tp, W, cont);
+        } else {
+          constexpr bool CM = ACC == ACCM_COMP;
+          if (tp.kj) sym_cube_istream4<C, T, R, true, CM>(tile, ob, lt, tp, S4, cont);
+          else sym_cube_istream4<C, T, R, false, CM>(tile, ob, lt, tp, S4, cont);
+        }
       }
     } else if (active) {
       T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
@@ -936,7 +1186,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
 
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH = false, bool IST = false>
 int launch_sweep2(const SweepArgs &a, const Taps &tp, cudaStream_t s, int grid_cap = 0) {
-  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
+  typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST> C;
   static_assert(C::SMEM <= 227 * 1024, "tile too large");
   static_assert(BK * BJ * BI <= 8192 && C::TILE <= 16384, "plan entry fields overflow");
   auto kern = sweep2_kernel<T, BK, BJ, BI, R, FAM, ACC, BATCH, IST>;

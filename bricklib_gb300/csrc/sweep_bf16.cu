@@ -39,7 +39,14 @@ namespace bk {
 int sweep_dispatch_bf16(const SweepPlan &p, const SweepArgs &a, Taps &tp, cudaStream_t s) {
   if (p.v2) {
     if (p.shape == 0) {
-      // mirror-symmetric cubes: pair sums, fewer multiply-adds
+      // mirror-symmetric cubes: class sums streamed along i (native or compensated arithmetic)
+      if (p.sym && p.fam == FAM_CUBE && p.istream && (p.acc == ACCM_NATIVE || p.acc == ACCM_COMP)) {
+        if (p.acc == ACCM_NATIVE && p.r == 1) return launch_sweep2<__nv_bfloat16, 8, 8, 8, 1, FAM_CUBESYM, ACCM_NATIVE, false, true>(a, tp, s);
+        if (p.acc == ACCM_NATIVE && p.r == 2) return launch_sweep2<__nv_bfloat16, 8, 8, 8, 2, FAM_CUBESYM, ACCM_NATIVE, false, true>(a, tp, s);
+        if (p.r == 1) return launch_sweep2<__nv_bfloat16, 8, 8, 8, 1, FAM_CUBESYM, ACCM_COMP, false, true>(a, tp, s);
+        if (p.r == 2) return launch_sweep2<__nv_bfloat16, 8, 8, 8, 2, FAM_CUBESYM, ACCM_COMP, false, true>(a, tp, s);
+      }
+      // ... one brick at a time on column pairs (BK_SWEEP_ISTREAM=0)
       if (p.sym && p.fam == FAM_CUBE && p.acc == ACCM_NATIVE) {
         if (p.symij && p.r == 1) return launch_sweep2<__nv_bfloat16, 8, 8, 8, 1, FAM_CUBESYM_IJ, ACCM_NATIVE>(a, tp, s);
         if (p.symij && p.r == 2) return launch_sweep2<__nv_bfloat16, 8, 8, 8, 2, FAM_CUBESYM_IJ, ACCM_NATIVE>(a, tp, s);

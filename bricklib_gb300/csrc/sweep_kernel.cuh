@@ -79,6 +79,8 @@ struct Taps {
   double c[BK_MAX_TAPS];
   float2 cp[TAP_PAIRS];    // (cf, cf) of the first taps: operands of packed FP32 arithmetic
   int kj;                  // mirror-symmetric cube also symmetric under the k <-> j swap
+  // mirror-symmetric cubes: (cf, cf) of class (|dk|, |dj|, |di|) at ((|dk| (R+1) + |dj|) (R+1) + |di|)
+  float2 sp[27];
 };
 
 __host__ __device__ constexpr int sweep_threads(int tpb) { return tpb < 128 ? 128 : tpb; }

@@ -31,6 +31,9 @@ class NotLinear(ValueError):
     pass
 
 
+SYMBOLIC: Dict = {}  # constants table that keeps every named constant as a C++ expression
+
+
 def _modules():
     """The st package of this front end, importable under the names scripts use."""
     mods = {}
@@ -56,11 +59,95 @@ def constants_from_header(path: str) -> Dict[str, float]:
     return out
 
 
-def _const(name: str, consts: Dict) -> float:
+class SymCoef:
+    """A coefficient linear in named constants -- {name: factor}, the empty name for the
+    literal part -- for lowering a script to C++ source, where ConstRef("coeff[5]") or
+    ConstRef("MPI_ALPHA") stay expressions of the caller's scope."""
+
+    def __init__(self, terms: Dict[str, float]):
+        self.t = {k: float(v) for k, v in terms.items() if v != 0.0}
+
+    @staticmethod
+    def of(x) -> "SymCoef":
+        return x if isinstance(x, SymCoef) else SymCoef({"": float(x)})
+
+    def literal(self) -> Optional[float]:
+        return self.t.get("", 0.0) if set(self.t) <= {""} else None
+
+    def __add__(self, o):
+        o = SymCoef.of(o)
+        t = dict(self.t)
+        for k, v in o.t.items():
+            t[k] = t.get(k, 0.0) + v
+        return SymCoef(t)
+
+    __radd__ = __add__
+
+    def __neg__(self):
+        return SymCoef({k: -v for k, v in self.t.items()})
+
+    def __sub__(self, o):
+        return self + (-SymCoef.of(o))
+
+    def __rsub__(self, o):
+        return SymCoef.of(o) - self
+
+    def __mul__(self, o):
+        o = SymCoef.of(o)
+        a, b = self.literal(), o.literal()
+        if a is None and b is None:
+            raise NotLinear("product of two named constants: give one of them a value")
+        if b is not None:
+            return SymCoef({k: v * b for k, v in self.t.items()})
+        return SymCoef({k: v * a for k, v in o.t.items()})
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        b = SymCoef.of(o).literal()
+        if b is None:
+            raise NotLinear("division by a named constant")
+        return SymCoef({k: v / b for k, v in self.t.items()})
+
+    def __eq__(self, o):
+        try:
+            o = SymCoef.of(o)
+        except (TypeError, ValueError):
+            return NotImplemented
+        return self.t == o.t
+
+    def __ne__(self, o):
+        r = self.__eq__(o)
+        return r if r is NotImplemented else not r
+
+    def __hash__(self):
+        return hash(tuple(sorted(self.t.items())))
+
+    def cpp(self) -> str:
+        """The coefficient as a C++ expression (names as written in the script)."""
+        if not self.t:
+            return "0.0"
+        parts = []
+        for k in sorted(self.t, key=lambda x: (x == "", x)):
+            v = self.t[k]
+            if k == "":
+                parts.append(repr(v))
+            elif v == 1.0:
+                parts.append(f"({k})")
+            elif v == -1.0:
+                parts.append(f"-({k})")
+            else:
+                parts.append(f"{v!r} * ({k})")
+        return " + ".join(parts).replace("+ -", "- ")
+
+
+def _const(name: str, consts: Dict):
     try:
         return float(name)
     except ValueError:
         pass
+    if consts is SYMBOLIC:
+        return SymCoef({name.strip(): 1.0})
     if name in consts:
         return float(consts[name])
     m = re.fullmatch(r"\s*(\w+)\s*\[\s*(\d+)\s*\]\s*", name)
@@ -160,6 +247,16 @@ def _strip_ops(expr, consts):
 def load_stencil(path: str, constants: Optional[Dict] = None, name: Optional[str] = None,
                  input_grid: Optional[str] = None) -> stencils.Stencil:
     """Run a stencil script and lower its (single) output grid to a Stencil."""
+    low = lower_script(path, constants, input_grid)
+    st = stencils.custom(name or os.path.splitext(os.path.basename(path))[0], low["taps"], low["coeff"])
+    st.pre_op, st.post_op = low["pre_op"], low["post_op"]
+    return st
+
+
+def lower_script(path: str, constants: Optional[Dict] = None, input_grid: Optional[str] = None) -> Dict:
+    """Run a stencil script and lower its output grid: {"taps": [(dk, dj, di), ...], "coeff":
+    [...], "pre_op", "post_op", "input": name, "output": name}.  With constants=SYMBOLIC every
+    named constant stays a SymCoef (a C++ expression of the caller's scope)."""
     _modules()
     ns: Dict = {"__name__": "__stencil__", "__file__": path}
     with open(path) as f:
@@ -182,12 +279,12 @@ def load_stencil(path: str, constants: Optional[Dict] = None, name: Optional[str
         grids = [g for g in grids if g.name == input_grid]
     if len(grids) != 1:
         raise ValueError("the script must declare exactly one input grid (or name it with input_grid)")
-    expr, pre, post = _strip_ops(expr, constants or {})
+    consts = constants if constants is not None else {}
+    expr, pre, post = _strip_ops(expr, consts)
     order: List[Tuple[int, int, int]] = []
-    c0, taps = _linear(expr, constants or {}, grids[0], order)
+    c0, taps = _linear(expr, consts, grids[0], order)
     if c0 != 0.0:
         raise NotLinear("affine term (a constant added to the stencil) is not supported")
     order = [t for t in order if taps.get(t, 0.0) != 0.0]
-    st = stencils.custom(name or os.path.splitext(os.path.basename(path))[0], order, [taps[t] for t in order])
-    st.pre_op, st.post_op = pre, post
-    return st
+    return {"taps": order, "coeff": [taps[t] for t in order], "pre_op": pre, "post_op": post,
+            "input": grids[0].name, "output": out.name}

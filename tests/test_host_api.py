@@ -246,8 +246,8 @@ def test_periodic_adjacency_points_at_wrapped_interior_bricks(nb):
 def test_bench_instruction_counts_follow_the_symmetry_the_kernels_use():
     """bench.py's floating-point instructions per point (the numerator of roofline.compute
     pipe_frac) follow the coefficient symmetry the kernels exploit: FP64 mirror-symmetric cubes
-    stream along i (37 with k <-> j symmetry, 43 without), FP32 ones sum classes on column pairs,
-    a cube without the symmetry takes a multiply-add per tap."""
+    stream along i (37 with k <-> j symmetry, 43 without), FP32 / BF16 ones too (compensated:
+    Dot2 W sums), a cube without the symmetry takes a multiply-add per tap."""
     import sys
     sys.path.insert(0, ROOT)
     import bench
@@ -256,7 +256,11 @@ def test_bench_instruction_counts_follow_the_symmetry_the_kernels_use():
     assert bench.fp_instructions_per_point(stencils.make("cube125", 3), nat, _abi.BK_F64) == 37.0
     assert bench.fp_instructions_per_point(_mirror_symmetric_cube(2, 5), nat, _abi.BK_F64) == 43.0
     assert bench.fp_instructions_per_point(_mirror_symmetric_cube(1, 5, kj=True), nat, _abi.BK_F64) == 13.0
-    assert bench.fp_instructions_per_point(_mirror_symmetric_cube(2, 5, ij=True), nat, _abi.BK_F32) == 58.5
+    assert bench.fp_instructions_per_point(stencils.make("cube125", 3), nat, _abi.BK_F32) == 37.0
+    assert bench.fp_instructions_per_point(_mirror_symmetric_cube(2, 5), nat, _abi.BK_BF16) == 43.0
+    assert bench.fp_instructions_per_point(_mirror_symmetric_cube(1, 5), nat, _abi.BK_F32) == 14.0
+    assert bench.fp_instructions_per_point(stencils.make("cube125", 3), _abi.BK_ACC_COMPENSATED,
+                                           _abi.BK_F32) == 15 + 3 * 52 + 22
     assert bench.fp_instructions_per_point(stencils.make("cube27", 3), nat, _abi.BK_F64) == 27.0
     assert bench.fp_instructions_per_point(stencils.make("star25", 3), nat, _abi.BK_F64) == 25.0
     assert bench.fp_instructions_per_point(stencils.make("cube125", 3), _abi.BK_ACC_FLOATFLOAT, _abi.BK_F64) == 125.0
