@@ -49,7 +49,8 @@ BK_OP_NONE, BK_OP_RELU, BK_OP_ABS = 0, 1, 2
 class bk_batch_domain(C.Structure):
     _fields_ = [("adj", C.c_void_p), ("nbricks", C.c_uint), ("dat", C.c_void_p), ("chunks", C.c_long),
                 ("step", C.c_size_t), ("off0", C.c_size_t), ("off1", C.c_size_t), ("blist", C.c_void_p),
-                ("nlist", C.c_uint), ("pairs", C.c_void_p), ("npairs", C.c_uint), ("stencil", C.c_int)]
+                ("nlist", C.c_uint), ("pairs", C.c_void_p), ("npairs", C.c_uint), ("stencil", C.c_int),
+                ("n", C.c_long * 3), ("gdims", C.c_long * 3), ("grid", C.c_void_p)]
 
 
 class bk_layout4(C.Structure):
@@ -128,6 +129,7 @@ SIGNATURES = {
                                   _P(bk_layout), C.c_int, C.c_int]),
     "bk_batch_set_grid": (C.c_int, [_vp, C.c_int]),
     "bk_batch_run": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "bk_batch_set_concurrent": (C.c_int, [_vp, C.c_int]),
     "bk_batch_parity": (C.c_int, [_vp]),
     "bk_batch_is_arena": (C.c_int, [_vp]),
     "bk_batch_destroy": (C.c_int, [_vp]),

@@ -76,7 +76,16 @@ def periodic_adjacency(adj: np.ndarray, pairs: np.ndarray) -> np.ndarray:
 
 
 def layout_valid(w: Workload, lay: B.Layout) -> bool:
-    return all(d.n[a] % lay.bdim[a] == 0 and d.n[a] >= lay.bdim[a] for d in w.domains for a in range(3))
+    """Every domain fits the brick dims: edges that are not whole bricks are padded to whole
+    bricks (the periodic boundary then runs as a cell-level wrap fill), which needs every
+    stencil radius within one brick and within the domain."""
+    rmax = max(s.radius for s in w.stencils)
+    return all(rmax <= lay.bdim[a] and rmax <= d.n[a] for d in w.domains for a in range(3))
+
+
+def partial(spec: DomainSpec, lay: B.Layout) -> bool:
+    """Whether some edge of the domain is not a whole number of bricks."""
+    return any(spec.n[a] % lay.bdim[a] for a in range(3))
 
 
 class DomainStorage:
@@ -90,18 +99,26 @@ class DomainStorage:
 
     @staticmethod
     def bricks(spec: DomainSpec, lay: B.Layout) -> int:
-        return int(np.prod([spec.n[a] // lay.bdim[a] + 2 for a in range(3)]))
+        return int(np.prod([-(-spec.n[a] // lay.bdim[a]) + 2 for a in range(3)]))
 
     def __init__(self, spec: DomainSpec, lay: B.Layout, dtype: int, wrap: bool = False,
                  storage: Optional[B.BrickStorage] = None):
         self.spec, self.lay, self.dtype = spec, lay, dtype
-        nb = tuple(spec.n[a] // lay.bdim[a] for a in range(3))
+        # a domain whose edges are not whole bricks is padded to whole bricks; its periodic
+        # boundary is then the batch's cell-level wrap fill (the ghost bricks hold the wrapped
+        # cells), not the adjacency or a brick-pair plan
+        self.partial = partial(spec, lay)
+        nb = tuple(-(-spec.n[a] // lay.bdim[a]) for a in range(3))
         self.gdims = tuple(x + 2 for x in nb)
         self.grid, info = B.init_grid(list(reversed(self.gdims)))
         self.nbricks = info.nbricks
         g3 = self.grid.reshape(self.gdims)
         self.interior = np.ascontiguousarray(g3[1:-1, 1:-1, 1:-1].reshape(-1))
-        pairs = B.GhostPlan.periodic(self.grid, nb, (1, 1, 1)).host
+        if self.partial:
+            pairs = np.zeros((0, 2), dtype=np.uint32)
+            wrap = False
+        else:
+            pairs = B.GhostPlan.periodic(self.grid, nb, (1, 1, 1)).host
         if wrap:
             info = B.BrickInfo(self.nbricks, periodic_adjacency(info.adj, pairs))
             pairs = np.zeros((0, 2), dtype=np.uint32)
@@ -122,7 +139,24 @@ class DomainStorage:
         d.blist, d.nlist = self.interior.ctypes.data, len(self.interior)
         d.pairs, d.npairs = self.pairs.ctypes.data, len(self.pairs)
         d.stencil = stencil
+        if self.partial:
+            d.n = (C.c_long * 3)(*self.spec.n)
+            d.gdims = (C.c_long * 3)(*self.gdims)
+            d.grid = self.grid.ctypes.data
         return d
+
+    def cells(self, which: int) -> np.ndarray:
+        """Field `which` of the domain as an array of its cells (k, j, i), read back to the host."""
+        host = B.movBrickStorage(self.storage, to_device=False).host.reshape(self.nbricks, -1)
+        lay = self.lay
+        f = host[:, which * lay.size:(which + 1) * lay.size]
+        off = lay.offsets().reshape(lay.bdim)  # element offset of (k, j, i) in a brick
+        nb = [g - 2 for g in self.gdims]
+        g3 = self.grid.reshape(self.gdims)[1:-1, 1:-1, 1:-1]
+        full = f[g3.reshape(-1)][:, off.reshape(-1)].reshape(nb + list(lay.bdim))
+        full = full.transpose(0, 3, 1, 4, 2, 5).reshape([nb[a] * lay.bdim[a] for a in range(3)])
+        n = self.spec.n
+        return full[:n[0], :n[1], :n[2]]
 
 
 class Batch:
@@ -215,9 +249,12 @@ def time_batch(b: Batch, steps: int, reps: int = 3, stream=None) -> float:
 
 
 def autotune(w: Workload, dtype: int = BK_F32, acc: int = BK_ACC_NATIVE, steps: int = 10,
-             candidates=CANDIDATES, grid_caps=(0, 152 * 8, 152 * 4), use_cache: bool = True) -> Dict:
-    """Time every valid (brick dims, fold) candidate and CTA cap on the workload; return the
-    best with the full table.  Results are cached per (workload, dtype, acc, GPU)."""
+             candidates=CANDIDATES, grid_caps=(0,), concurrency=(1, 0), use_cache: bool = True) -> Dict:
+    """Time every (brick dims, fold) candidate -- domains whose edges are not whole bricks
+    padded to whole bricks with the cell-level wrap fill -- with the stencil segments of a step
+    as parallel graph branches or one after another (and any CTA caps given, which bound the
+    batch-mode kernels of domains in storages of their own); return the best with the full
+    table.  Results are cached per (workload, dtype, acc, GPU)."""
     import torch
     key = f"{w.signature()}:{dtype}:{acc}:{torch.cuda.get_device_name()}"
     cache = {}
@@ -232,14 +269,17 @@ def autotune(w: Workload, dtype: int = BK_F32, acc: int = BK_ACC_NATIVE, steps: 
     for bdim, fold in candidates:
         lay = B.Layout(bdim, fold)
         if not layout_valid(w, lay):
-            table.append({"bdim": bdim, "fold": fold, "skipped": "domain edges not multiples of the brick dims"})
+            table.append({"bdim": bdim, "fold": fold, "skipped": "a stencil radius exceeds a brick or a domain edge"})
             continue
         b = Batch(w, lay, dtype, acc)
-        for cap in grid_caps:
-            call("bk_batch_set_grid", b.h, cap)
-            t = time_batch(b, steps)
-            table.append({"bdim": bdim, "fold": fold, "grid_cap": cap, "s_per_run": t,
-                          "gstencil_s": w.points * steps / t / 1e9})
+        npart = sum(1 for ds in b.doms if ds.partial)
+        for conc in concurrency:
+            call("bk_batch_set_concurrent", b.h, conc)
+            for cap in grid_caps:
+                call("bk_batch_set_grid", b.h, cap)
+                t = time_batch(b, steps)
+                table.append({"bdim": bdim, "fold": fold, "concurrent": conc, "grid_cap": cap,
+                              "partial_domains": npart, "s_per_run": t, "gstencil_s": w.points * steps / t / 1e9})
         b.close()
         del b
     best = max((r for r in table if "gstencil_s" in r), key=lambda r: r["gstencil_s"])

@@ -125,6 +125,61 @@ batch_fill_kernel(const BatchDomain *__restrict__ doms, unsigned ndom, const uin
   }
 }
 
+// A domain whose cells are not whole bricks: its fields, brick grid (device) and cell counts.
+struct WrapDomain {
+  unsigned char *f0, *f1;
+  unsigned long long step_bytes;
+  const unsigned *grid;  // gk x gj x gi positions -> brick
+  long long chunks;
+  int g[3], n[3], r;     // brick grid (k, j, i) with one ghost brick per side, cells, stencil radius
+};
+
+// Cell-level periodic wrap of the input fields: every cell within r of a domain's box and
+// outside it takes the value at its periodic image (always a cell inside the box, which
+// nothing here writes).  Cell (z, y, x), z in [-r, n + r), sits in brick position
+// floor(z / bk) + 1 (the ghost layer is position 0).  One block row (blockIdx.y) per domain.
+template <typename W>
+__global__ void __launch_bounds__(256)
+wrap_fill_kernel(const WrapDomain *__restrict__ doms, unsigned ndom, int parity, Layout L, int *err) {
+  const unsigned d = blockIdx.y;
+  if (d >= ndom) return;
+  const WrapDomain D = doms[d];
+  const int r = D.r, e0 = D.n[0] + 2 * r, e1 = D.n[1] + 2 * r, e2 = D.n[2] + 2 * r;
+  const long long box = (long long)e0 * e1 * e2;
+  unsigned char *base = parity ? D.f1 : D.f0;
+  const int bd[3] = {L.bk, L.bj, L.bi};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < box; c += (long long)gridDim.x * blockDim.x) {
+    int q[3];
+    q[2] = (int)(c % e2) - r;
+    q[1] = (int)((c / e2) % e1) - r;
+    q[0] = (int)(c / ((long long)e2 * e1)) - r;
+    if (q[0] >= 0 && q[0] < D.n[0] && q[1] >= 0 && q[1] < D.n[1] && q[2] >= 0 && q[2] < D.n[2]) continue;
+    int pd[3], od[3], ps[3], os[3];
+    bool ok = true;
+    for (int a = 0; a < 3; ++a) {
+      const int w = ((q[a] % D.n[a]) + D.n[a]) % D.n[a];  // periodic image, in the box
+      pd[a] = (q[a] + bd[a]) / bd[a];                     // floor(q / b) + 1 for q >= -b
+      od[a] = q[a] + bd[a] - pd[a] * bd[a];
+      ps[a] = w / bd[a] + 1;
+      os[a] = w - (ps[a] - 1) * bd[a];
+      ok = ok && pd[a] >= 0 && pd[a] < D.g[a];
+    }
+    if (!ok) {  // a radius deeper than one ghost brick
+      atomicOr(err, FLAG_BOUNDS);
+      continue;
+    }
+    const unsigned bdst = D.grid[((long long)pd[0] * D.g[1] + pd[1]) * D.g[2] + pd[2]];
+    const unsigned bsrc = D.grid[((long long)ps[0] * D.g[1] + ps[1]) * D.g[2] + ps[2]];
+    if ((long long)bdst >= D.chunks || (long long)bsrc >= D.chunks) {
+      atomicOr(err, FLAG_BOUNDS);
+      continue;
+    }
+    const W *src = reinterpret_cast<const W *>(base + (size_t)bsrc * D.step_bytes) + L.offset(os[0], os[1], os[2]);
+    W *dst = reinterpret_cast<W *>(base + (size_t)bdst * D.step_bytes) + L.offset(od[0], od[1], od[2]);
+    *dst = *src;
+  }
+}
+
 template <typename T, int BK, int BJ, int BI, int R, int FAM, bool RM, int ACC>
 int launch_batch_sweep(const BatchDomain *doms, unsigned ndom, const uint2 *work, unsigned nwork, int parity,
                        const Taps &tp, const Layout &L, int *err, int grid_cap, cudaStream_t s) {
@@ -179,9 +234,9 @@ int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndo
   BK_B2(BK_, BJ_, BI_, 1, FAM_STAR) BK_B2(BK_, BJ_, BI_, 2, FAM_STAR) BK_B2(BK_, BJ_, BI_, 4, FAM_STAR) \
   BK_B2(BK_, BJ_, BI_, 1, FAM_CUBE) BK_B2(BK_, BJ_, BI_, 2, FAM_CUBE)
     if (p.shape == 0) {
-      if constexpr (sizeof(T) <= 4 && (ACC == ACCM_NATIVE || ACC == ACCM_COMP)) {
-        // mirror-symmetric cubes on 4-byte storage: the class sums of the plain sweep's stream, one
-        // brick at a time (the same bits as the plain sweep of the same bricks)
+      if constexpr ((sizeof(T) <= 4 && (ACC == ACCM_NATIVE || ACC == ACCM_COMP)) || (sizeof(T) == 8 && ACC == ACCM_NATIVE)) {
+        // mirror-symmetric cubes: the class sums streamed along each domain's runs of bricks, as
+        // the plain sweep streams them (the same bits as the plain sweep of the same bricks)
         if (p.sym && p.fam == FAM_CUBE && p.r == 1) return launch_sweep2<T, 8, 8, 8, 1, FAM_CUBESYM, ACC, true, true>(a, tp, s, grid_cap);
         if (p.sym && p.fam == FAM_CUBE && p.r == 2) return launch_sweep2<T, 8, 8, 8, 2, FAM_CUBESYM, ACC, true, true>(a, tp, s, grid_cap);
       }
@@ -195,6 +250,8 @@ int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndo
     }
     if constexpr (ACC == ACCM_NATIVE && sizeof(T) == 4) {
       if (p.shape == 1) { BK_B2SET(4, 4, 4) }
+    }
+    if constexpr (ACC == ACCM_NATIVE) {  // FP32 and FP64: the brick dims the autotuner tries
       if (p.shape == 2) { BK_B2SET(16, 8, 8) }
       if (p.shape == 3) { BK_B2SET(8, 8, 32) }
     }
@@ -258,6 +315,21 @@ struct bk_batch {
   std::vector<bk_stencil> csts;
   int acc_mode = BK_ACC_NATIVE;
   bk_layout lay{};
+  // The stencil segments of a step are independent (each writes its own domains' bricks):
+  // with `concurrent` they run as parallel branches -- one stream each, forked from the
+  // caller's stream and joined before the next step -- so one segment's last wave overlaps
+  // the others' work, in a captured graph as in eager runs.
+  int concurrent = 1;
+  std::vector<cudaStream_t> lanes;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  // domains of partial bricks: their descriptors and brick grids on the device, the cells of
+  // the largest wrap box (the fill's grid size)
+  WrapDomain *d_wrap = nullptr;
+  unsigned *d_wgrid = nullptr;
+  unsigned nwrap = 0;
+  long long wrap_cells = 0;
+  std::vector<int> radius;  // per stencil
 };
 
 namespace bk {
@@ -293,30 +365,79 @@ int batch_launch_fill(const BatchDomain *doms, unsigned ndom, const uint3 *pairs
   return BK_OK;
 }
 
+static int batch_sweep_segment(bk_batch *b, size_t q, cudaStream_t s);
+
+// Stencil radius of a batch stencil (the depth of the wrap fill).
+static int wrap_radius(const bk_batch *b, int stencil) { return b->radius[stencil]; }
+
+// Streams and events of the parallel segment branches (made on first use).
+static int batch_lanes(bk_batch *b) {
+  const size_t n = b->seg.size();
+  if (b->lanes.size() == n) return BK_OK;
+  if (!b->fork) BK_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  while (b->lanes.size() < n) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    BK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    b->lanes.push_back(st);
+    BK_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    b->joins.push_back(ev);
+  }
+  return BK_OK;
+}
+
 static int batch_sweep(bk_batch *b, cudaStream_t s) {
-  if (b->arena) {
-    const bk_field &fin = b->field[b->parity], &fout = b->field[b->parity ^ 1];
-    for (size_t q = 0; q < b->sts.size(); ++q) {
-      const unsigned first = b->seg[q].first, count = b->seg[q].second;
-      if (!count) continue;
-      const int st = bk_sweep(b->d_gadj, b->total, &fin, &fout, b->d_gwork + first, count, &b->csts[q], &b->lay,
-                              b->acc_mode, s);
-      if (st) return st;
+  size_t live = 0;
+  for (const auto &sg : b->seg) live += sg.second ? 1 : 0;
+  if (b->concurrent && live > 1) {
+    int st = batch_lanes(b);
+    if (st) return st;
+    BK_CUDA(cudaEventRecord(b->fork, s));
+    for (size_t q = 0; q < b->seg.size(); ++q) {
+      if (!b->seg[q].second) continue;
+      BK_CUDA(cudaStreamWaitEvent(b->lanes[q], b->fork, 0));
+      if ((st = batch_sweep_segment(b, q, b->lanes[q]))) return st;
+      BK_CUDA(cudaEventRecord(b->joins[q], b->lanes[q]));
+      BK_CUDA(cudaStreamWaitEvent(s, b->joins[q], 0));
     }
     return BK_OK;
   }
-  for (size_t q = 0; q < b->sts.size(); ++q) {
-    const unsigned first = b->seg[q].first, count = b->seg[q].second;
-    if (!count) continue;
-    const uint2 *work = b->d_work + first;
-    const int st = batch_launch_sweep(b->sts[q], b->dtype, b->d_doms, b->ndom, work, count, b->parity, b->L, b->err,
-                                      b->grid_cap, b->aligned, s);
+  for (size_t q = 0; q < b->seg.size(); ++q) {
+    const int st = batch_sweep_segment(b, q, s);
     if (st) return st;
   }
   return BK_OK;
 }
 
+// One stencil segment of a step: a plain sweep over the arena's global list, or the batch-mode
+// kernel over (domain, brick) work items.
+static int batch_sweep_segment(bk_batch *b, size_t q, cudaStream_t s) {
+  const unsigned first = b->seg[q].first, count = b->seg[q].second;
+  if (!count) return BK_OK;
+  if (b->arena) {
+    const bk_field &fin = b->field[b->parity], &fout = b->field[b->parity ^ 1];
+    return bk_sweep(b->d_gadj, b->total, &fin, &fout, b->d_gwork + first, count, &b->csts[q], &b->lay, b->acc_mode, s);
+  }
+  return batch_launch_sweep(b->sts[q], b->dtype, b->d_doms, b->ndom, b->d_work + first, count, b->parity, b->L,
+                            b->err, b->grid_cap, b->aligned, s);
+}
+
+static int batch_wrap_fill(bk_batch *b, cudaStream_t s) {
+  if (!b->nwrap) return BK_OK;
+  const unsigned bx = (unsigned)std::min<long long>((b->wrap_cells + 255) / 256, 64);
+  const dim3 grid(bx, b->nwrap);
+  const size_t es = dtype_size(b->dtype);
+  if (es == 8) wrap_fill_kernel<unsigned long long><<<grid, 256, 0, s>>>(b->d_wrap, b->nwrap, b->parity, b->L, b->err);
+  else if (es == 4) wrap_fill_kernel<unsigned><<<grid, 256, 0, s>>>(b->d_wrap, b->nwrap, b->parity, b->L, b->err);
+  else wrap_fill_kernel<unsigned short><<<grid, 256, 0, s>>>(b->d_wrap, b->nwrap, b->parity, b->L, b->err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "batch wrap fill launch");
+  return BK_OK;
+}
+
 static int batch_fill(bk_batch *b, cudaStream_t s) {
+  int st = batch_wrap_fill(b, s);
+  if (st) return st;
   if (b->arena) return b->ngpairs ? bk_ghost_fill(b->d_gpairs, b->ngpairs, &b->field[b->parity], &b->lay, s) : BK_OK;
   if (!b->npairs) return BK_OK;
   const size_t bytes = (size_t)b->L.size() * dtype_size(b->dtype);
@@ -333,6 +454,16 @@ static int batch_fill(bk_batch *b, cudaStream_t s) {
 static void batch_free(bk_batch *b) {
   for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
   b->graphs.clear();
+  if (b->d_wrap) cudaFree(b->d_wrap);
+  if (b->d_wgrid) cudaFree(b->d_wgrid);
+  b->d_wrap = nullptr;
+  b->d_wgrid = nullptr;
+  for (auto st : b->lanes) cudaStreamDestroy(st);
+  for (auto ev : b->joins) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  b->lanes.clear();
+  b->joins.clear();
+  b->fork = nullptr;
   if (b->d_doms) cudaFree(b->d_doms);
   if (b->d_work) cudaFree(b->d_work);
   if (b->d_pairs) cudaFree(b->d_pairs);
@@ -461,10 +592,18 @@ int bk_batch_create(bk_batch **out, const bk_batch_domain *doms, unsigned ndom, 
     }
   }
   b->acc = b->sts[0].plan.acc;
+  for (unsigned q = 0; q < nst; ++q) {
+    int r = 0;
+    for (int t = 0; t < sts[q].npoints; ++t)
+      for (int a = 0; a < 3; ++a) r = std::max(r, std::abs(sts[q].offsets[t][a]));
+    b->radius.push_back(r);
+  }
   // domain table, work list sorted by stencil, fill list
   std::vector<BatchDomain> hd(ndom);
   std::vector<std::vector<uint2>> per_st(nst);
   std::vector<uint3> pairs;
+  std::vector<WrapDomain> wdoms;
+  std::vector<unsigned> wgrids;
   const size_t es = dtype_size(dtype);
   for (unsigned d = 0; d < ndom; ++d) {
     const bk_batch_domain &D = doms[d];
@@ -477,6 +616,35 @@ int bk_batch_create(bk_batch **out, const bk_batch_domain *doms, unsigned ndom, 
     }
     unsigned char *base = reinterpret_cast<unsigned char *>(D.dat);
     hd[d] = BatchDomain{D.adj, D.nbricks, (unsigned)D.stencil, base + D.off0 * es, base + D.off1 * es, D.step * es, D.chunks};
+    if (D.n[0] || D.n[1] || D.n[2]) {
+      const int bdim[3] = {L.bk, L.bj, L.bi};
+      bool ok = D.grid != nullptr;
+      for (int a = 0; a < 3 && ok; ++a)
+        ok = D.n[a] > 0 && D.gdims[a] == (D.n[a] + bdim[a] - 1) / bdim[a] + 2 && wrap_radius(b, D.stencil) <= bdim[a] &&
+             wrap_radius(b, D.stencil) <= D.n[a];
+      if (!ok) {
+        delete b;
+        return fail(BK_ERR_ARG, "bk_batch_create: domain " + std::to_string(d) +
+                                    ": partial bricks need the grid, n cells per axis (at least the stencil radius) "
+                                    "and gdims = n / bdim rounded up + 2 (stencil radius at most a brick)");
+      }
+      WrapDomain w{};
+      w.f0 = base + D.off0 * es;
+      w.f1 = base + D.off1 * es;
+      w.step_bytes = D.step * es;
+      w.chunks = D.chunks;
+      w.r = wrap_radius(b, D.stencil);
+      for (int a = 0; a < 3; ++a) {
+        w.g[a] = (int)D.gdims[a];
+        w.n[a] = (int)D.n[a];
+      }
+      const size_t gsize = (size_t)D.gdims[0] * D.gdims[1] * D.gdims[2];
+      w.grid = reinterpret_cast<const unsigned *>(wgrids.size());  // offset, rebased after the upload
+      wgrids.insert(wgrids.end(), D.grid, D.grid + gsize);
+      wdoms.push_back(w);
+      b->wrap_cells = std::max<long long>(b->wrap_cells, (long long)(w.n[0] + 2 * w.r) * (w.n[1] + 2 * w.r) *
+                                                             (w.n[2] + 2 * w.r));
+    }
     if ((reinterpret_cast<uintptr_t>(base) | (D.off0 * es) | (D.off1 * es) | (D.step * es)) % 16) b->aligned = false;
     for (unsigned n = 0; n < D.nlist; ++n) per_st[D.stencil].push_back(make_uint2(d, D.blist[n]));
     for (unsigned p = 0; p < D.npairs; ++p) pairs.push_back(make_uint3(d, D.pairs[2 * p], D.pairs[2 * p + 1]));
@@ -496,6 +664,14 @@ int bk_batch_create(bk_batch **out, const bk_batch_domain *doms, unsigned ndom, 
   if (e == cudaSuccess) e = cudaMemcpy(b->d_doms, hd.data(), sizeof(BatchDomain) * ndom, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && work.size()) e = cudaMemcpy(b->d_work, work.data(), sizeof(uint2) * work.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && pairs.size()) e = cudaMemcpy(b->d_pairs, pairs.data(), sizeof(uint3) * pairs.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && wdoms.size()) {
+    e = cudaMalloc(&b->d_wgrid, sizeof(unsigned) * wgrids.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_wgrid, wgrids.data(), sizeof(unsigned) * wgrids.size(), cudaMemcpyHostToDevice);
+    for (auto &w : wdoms) w.grid = b->d_wgrid + reinterpret_cast<size_t>(w.grid);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_wrap, sizeof(WrapDomain) * wdoms.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_wrap, wdoms.data(), sizeof(WrapDomain) * wdoms.size(), cudaMemcpyHostToDevice);
+    b->nwrap = (unsigned)wdoms.size();
+  }
   if (e != cudaSuccess) {
     batch_free(b);
     delete b;
@@ -568,6 +744,14 @@ int bk_batch_run(bk_batch *b, int steps, int fill_every, int use_graph, void *st
   }
   BK_CUDA(cudaGraphLaunch(it->second, user));
   if (steps % 2) b->parity ^= 1;
+  return BK_OK;
+}
+
+int bk_batch_set_concurrent(bk_batch *b, int on) {
+  if (!b) return fail(BK_ERR_ARG, "bk_batch_set_concurrent: bad arguments");
+  b->concurrent = on ? 1 : 0;
+  for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
+  b->graphs.clear();
   return BK_OK;
 }
 

@@ -112,14 +112,20 @@ struct Sweep2Cfg {
   static constexpr bool PERM = ES == 8 && BI == 8;
   static constexpr int NEED = BI + 2 * RP;
   // the class-sum stream of 4- / 2-byte storage reads 4 columns of 32 rows at once (16 / 8
-  // bytes per lane): rows of 20 FP32 elements put the 8 rows of a quarter warp in distinct
-  // 4-bank groups (16-byte reads, conflict free); BF16 rows of 24 (two-way within a half warp,
-  // which reads half the bytes of the FP32 case)
+  // bytes per lane).  FP32: rows of 16 elements with the 16-byte units of row jj XOR-permuted by
+  // (jj >> 1) & 3 (SWZ), which puts the 8 rows of a quarter warp in distinct 4-bank groups
+  // (conflict free) with no padding -- a smaller tile, more CTAs per SM.  BF16: rows of 24
+  // (two-way within a half warp, which reads half the bytes of the FP32 case)
   static constexpr bool CS4 = IST && ES <= 4;
-  static constexpr int EI = CS4 ? (ES == 4 ? 20 : 24)
+  static constexpr bool SWZ = CS4 && ES == 4 && BI + 2 * RP == 16;
+  static constexpr int EI = CS4 ? (ES == 4 ? (SWZ ? 16 : 20) : 24)
                           : PERM ? (NEED % 8 <= 4 ? NEED - NEED % 8 + 4 : NEED - NEED % 8 + 12)
                                  : conflict_free_row(NEED, BI, ES, VE);
   static constexpr int TILE = EK * EJ * EI;  // elements per brick tile
+  // position within tile row jj of column ii (SWZ: the row's 16-byte units permuted)
+  static __host__ __device__ __forceinline__ int col(int jj, int ii) {
+    return SWZ ? ((((ii >> 2) ^ ((jj >> 1) & 3)) << 2) | (ii & 3)) : ii;
+  }
   static constexpr int TILE_BYTES = (TILE * ES + 15) / 16 * 16;
   // Column pairs: one warp per 8x8x8 brick, each lane computing columns (i0, i0 + 1) from
   // 8-byte (FP32) / 4-byte (BF16) row loads, for the cubes whose per-plane row values or
@@ -218,7 +224,7 @@ __device__ __forceinline__ unsigned plan_entry(int g) {
   const int lk = kk - R - qk * BK, lj = jj - R - qj * BJ, li = ii - C::RP - qi * BI;
   const unsigned slot = (unsigned)((qk + 1) * 9 + (qj + 1) * 3 + (qi + 1));
   const unsigned src = (unsigned)((lk * BJ + lj) * BI + li);
-  const unsigned dst = (unsigned)((kk * C::EJ + jj) * C::EI + ii);
+  const unsigned dst = (unsigned)((kk * C::EJ + jj) * C::EI + C::col(jj, ii));
   return slot | (src << 5) | (dst << 18);
 }
 
@@ -544,17 +550,17 @@ struct CsWin {
 };
 
 // W_a (and errors) of the four tile columns c0 .. c0 + 3 for both rows of this lane.
-// base: tile element (plane k0, row j, column 0), i.e. brick-local (k0 - R, j - R, -RP).
+// base: tile row j of plane k0 (brick-local (k0 - R, j - R)); rows j .. j + 2R are read.
 template <typename C, typename T, int R, bool KJ, bool COMP>
-__device__ __forceinline__ void cs_group(const T *base, const int c0, const Taps &tp, float2 (&W)[2][R + 1][2],
-                                         float2 (&E)[COMP ? 2 : 1][R + 1][2]) {
+__device__ __forceinline__ void cs_group(const T *base, const int j, const int c0, const Taps &tp,
+                                         float2 (&W)[2][R + 1][2], float2 (&E)[COMP ? 2 : 1][R + 1][2]) {
   constexpr int SK = C::EJ * C::EI, SJ = C::EI;
   float2 Q[2][R + 1][R + 1][2];  // [o][c][b][pair]
 #pragma unroll
   for (int q = 0; q < 2 * R + 2; ++q) {  // tile plane k0 + q: brick-local plane k0 - R + q
     float2 v[2 * R + 1][2];
 #pragma unroll
-    for (int rr = 0; rr <= 2 * R; ++rr) ld_quad(base + q * SK + rr * SJ + c0, v[rr][0], v[rr][1]);
+    for (int rr = 0; rr <= 2 * R; ++rr) ld_quad(base + q * SK + rr * SJ + C::col(j + rr, c0), v[rr][0], v[rr][1]);
     float2 H[R + 1][2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -629,11 +635,11 @@ __device__ __forceinline__ float cs_at(const float2 (&P)[NO][R + 1][2], const fl
   return (m & 1) ? v.y : v.x;
 }
 
-// Outputs of the current group's four columns for both rows, parked in the tile (park: tile
-// element (plane k0 + R, row j + R) at the group's first column).
+// Outputs of the current group's four columns c0 .. c0 + 3 for both rows, parked in the tile at
+// their own input positions (park: tile row prow = j + R of plane k0 + R).
 template <typename C, typename T, int R, bool COMP>
-__device__ __forceinline__ void cs_out(T *park, const CsWin<R, COMP> &S, const float2 (&Wn)[2][R + 1][2],
-                                       const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
+__device__ __forceinline__ void cs_out(T *park, const int prow, const int c0, const CsWin<R, COMP> &S,
+                                       const float2 (&Wn)[2][R + 1][2], const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
   constexpr int SK = C::EJ * C::EI;
 #pragma unroll
   for (int o = 0; o < 2; ++o)
@@ -655,7 +661,7 @@ __device__ __forceinline__ void cs_out(T *park, const CsWin<R, COMP> &S, const f
         }
         v = sm + (cm + es);
       }
-      st_elem(park + o * SK + t, v);
+      st_elem(park + o * SK + C::col(prow, c0 + t), v);
     }
 }
 
@@ -691,15 +697,15 @@ __device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, 
   T *park = rt + (k0 + R) * SK + (j + R) * SJ;
   float2 Wn[2][R + 1][2], En[COMP ? 2 : 1][R + 1][2];
   if (!cont) {
-    cs_group<C, T, R, KJ, COMP>(base, RP - 4, tp, S.p, S.ep);
-    cs_group<C, T, R, KJ, COMP>(base, RP, tp, S.c, S.ec);
+    cs_group<C, T, R, KJ, COMP>(base, j, RP - 4, tp, S.p, S.ep);
+    cs_group<C, T, R, KJ, COMP>(base, j, RP, tp, S.c, S.ec);
   }
-  cs_group<C, T, R, KJ, COMP>(base, RP + 4, tp, Wn, En);
+  cs_group<C, T, R, KJ, COMP>(base, j, RP + 4, tp, Wn, En);
   __syncwarp();  // every lane is past its reads of columns RP .. RP + 7
-  cs_out<C, T, R, COMP>(park + RP, S, Wn, En);
+  cs_out<C, T, R, COMP>(park, j + R, RP, S, Wn, En);
   cs_shift<R, COMP>(S, Wn, En);
-  cs_group<C, T, R, KJ, COMP>(base, RP + 8, tp, Wn, En);  // the i-hi columns: never parked over
-  cs_out<C, T, R, COMP>(park + RP + 4, S, Wn, En);
+  cs_group<C, T, R, KJ, COMP>(base, j, RP + 8, tp, Wn, En);  // the i-hi columns: never parked over
+  cs_out<C, T, R, COMP>(park, j + R, RP + 4, S, Wn, En);
   cs_shift<R, COMP>(S, Wn, En);
   __syncwarp();  // the parked outputs of every lane are in the tile
   constexpr int AL = 4 * (int)sizeof(T);
@@ -707,13 +713,13 @@ __device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, 
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int e = q * 128 + 4 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
-      st_quad(ob + e, rt + (k + R) * SK + (jj + R) * SJ + RP + i);
+      st_quad(ob + e, rt + (k + R) * SK + (jj + R) * SJ + C::col(jj + R, RP + i));
     }
   } else {
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int e = q * 32 + lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
-      ob[e] = rt[(k + R) * SK + (jj + R) * SJ + RP + i];
+      ob[e] = rt[(k + R) * SK + (jj + R) * SJ + C::col(jj + R, RP + i)];
     }
   }
 }
@@ -987,12 +993,12 @@ __global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST>::NT
 sweep2_kernel(const SweepArgs a, const Taps tp) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST> C;
   constexpr int TPB = C::TPB, NB = C::NB, EPT = C::EPT;
-  static_assert(!IST || (C::ES == 8 && C::PAIR && NB == 1 && !BATCH && (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ)) ||
+  static_assert(!IST || (C::ES == 8 && C::PAIR && NB == 1 && (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ)) ||
                     (C::ES <= 4 && C::CS4 && NB == 1 && FAM == FAM_CUBESYM && ACC != ACCM_FF),
-                "class-sum streams: FP64 mirror-symmetric cubes on plain lists, or FP32 / BF16 ones (batch mode: "
-                "one brick at a time), one brick per CTA");
-  // 4- / 2-byte storage: a stream along the list in plain mode; brick by brick in batch mode
-  constexpr bool STREAM = IST && !BATCH;
+                "class-sum streams: mirror-symmetric cubes, FP64 (native) or FP32 / BF16 storage, one brick per CTA");
+  // streams run along the list, plain or batch mode (in batch mode a stream continues only
+  // within one domain's field)
+  constexpr bool STREAM = IST;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char *raw0 = smem_raw;                               // [NB] tiles, buffer 0
@@ -1013,10 +1019,30 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   }
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
-  // this CTA's groups: g0, g0 + gstride, ... below gend
-  const long long g0 = STREAM ? (long long)blockIdx.x * ngroups / gridDim.x : (long long)blockIdx.x;
-  const long long gend = STREAM ? ((long long)blockIdx.x + 1) * ngroups / gridDim.x : ngroups;
-  const long long gstride = STREAM ? 1 : (long long)gridDim.x;
+  // This CTA's groups.  Plain: every gridDim.x-th.  Streams of 4- / 2-byte storage: chunks of
+  // CH consecutive groups, chunk c to CTA c mod gridDim.x, so that at any time the CTAs work on
+  // neighbouring stretches of the list in step -- the j and k neighbours a brick's tile reads
+  // were just read by the CTAs on the neighbouring rows and are still in L2 (with a contiguous
+  // share per CTA they came many bricks apart in time, and the kernel read 2.6 times its
+  // algorithmic bytes from DRAM); CH is about 16, chosen so the chunks fill whole rounds.
+  // FP64 streams, bound by the FP64 pipe, keep one contiguous share per CTA (fewer stream
+  // restarts, each of which computes 2R more columns).
+  constexpr bool CHUNKED = STREAM && C::ES <= 4;
+  const long long G = gridDim.x;
+  long long CH = 1;
+  if constexpr (CHUNKED) {
+    const long long rounds = (ngroups + G * 16 - 1) / (G * 16);
+    CH = (ngroups + G * rounds - 1) / (G * rounds);
+    if (CH < 1) CH = 1;
+  }
+  auto next_group = [&](long long g) -> long long {
+    if constexpr (CHUNKED) return ((g + 1) % CH) ? g + 1 : g + 1 + (G - 1) * CH;
+    else if constexpr (STREAM) return g + 1;
+    else return g + G;
+  };
+  const long long g0 = CHUNKED ? (long long)blockIdx.x * CH
+                       : STREAM ? (long long)blockIdx.x * ngroups / G : (long long)blockIdx.x;
+  const long long gend = STREAM && !CHUNKED ? ((long long)blockIdx.x + 1) * ngroups / G : ngroups;
 
   // Adjacency of a group: fetched into registers two groups ahead (its global-load latency
   // hides under the current group's compute), stored into one of three nbrs slots.
@@ -1092,7 +1118,27 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     }
   };
   // issue the asynchronous gather of the group staged in nbrs[ns] into raw buffer buf
-  auto issue = [&](int buf, int ns) {
+  // Whether the stream continues from the group whose adjacency is in nbrs[prev] into the group
+  // in nbrs[ns]: both ran, and the latter's i-lo and centre columns of neighbours are the
+  // former's centre and i-hi columns (warp-uniform; lanes 0..17 check one slot pair each).
+  auto continues = [&](int prev, int ns) -> bool {
+    const unsigned *nb = nbrs + ns * 36, *pv = nbrs + prev * 36;
+    bool same = true;
+    if (lt < 18) {
+      const int s9 = lt < 9 ? lt : lt - 9, sh = lt < 9 ? 0 : 1;
+      const int base = (s9 / 3) * 9 + (s9 % 3) * 3;  // (dk, dj) = (s9 / 3 - 1, s9 % 3 - 1), di = -1
+      same = nb[base + sh] == pv[base + sh + 1];
+    }
+    // the same input field: in batch mode consecutive items may belong to different domains
+    same = same && *reinterpret_cast<const unsigned long long *>(nb + 28) ==
+                       *reinterpret_cast<const unsigned long long *>(pv + 28);
+    return __all_sync(0xFFFFFFFFu, same) && pv[27] != 0 && nb[27] != 0;
+  };
+  // issue the asynchronous gather of the group staged in nbrs[ns] into raw buffer buf; a
+  // continued stream reads only the tile columns from ICUT on (the W of the columns before
+  // come from the previous brick), so copies wholly before ICUT are skipped
+  constexpr int ICUT = !STREAM ? 0 : C::ES == 8 ? C::RP + R : C::RP + 4;
+  auto issue = [&](int buf, int ns, bool cont) {
     const unsigned *nbr = nbrs + (ns * NB + slot) * 36;
     if (nbr[27]) {
       unsigned char *tile = (buf ? raw1 : raw0) + slot * C::TILE_BYTES;
@@ -1104,6 +1150,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
         const unsigned p = plan[e];
         if (p != 0xFFFFFFFFu) {
           const unsigned sl = p & 31u, src = (p >> 5) & 8191u, dst = p >> 18;
+          if (STREAM && cont && C::col((int)(dst / C::EI) % C::EJ, (int)(dst % C::EI)) + C::VE <= ICUT) continue;
           const T *g = in + (size_t)nbr[sl] * step + src;
           cp_async<C::VB>(tbase + dst * C::ES, g);
         }
@@ -1116,22 +1163,22 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   long long grp = g0;
   fetch_adj(grp);
   store_adj(0);
-  fetch_adj(grp + gstride);
+  fetch_adj(next_group(grp));
   store_adj(1);
   __syncthreads();
-  issue(0, 0);
+  issue(0, 0, false);
 
   // i-streaming: W of the last 2R columns of the previous brick (sym_cube_istream), or of the
   // last two 4-column groups (sym_cube_istream4)
   double W[IST && C::ES == 8 ? 2 : 1][IST && C::ES == 8 ? R + 1 : 1][IST && C::ES == 8 ? 2 * R + 1 : 1];
   CsWin<R, ACC == ACCM_COMP> S4;
 
-  for (int it = 0; grp < gend; grp += gstride, ++it) {
+  for (int it = 0; grp < gend; grp = next_group(grp), ++it) {
     const int cur = it & 1, nxt = cur ^ 1;
     const int ncur = it % 3, nnxt = (it + 1) % 3, nfar = (it + 2) % 3;
     __syncthreads();     // nbrs[nnxt] visible; every thread is done with raw[nxt] and nbrs[nfar]
-    issue(nxt, nnxt);
-    fetch_adj(grp + 2 * gstride);  // lands while this group computes
+    issue(nxt, nnxt, STREAM && continues(ncur, nnxt));
+    fetch_adj(next_group(next_group(grp)));  // lands while this group computes
     cp_async_wait<1>();  // this thread's copies for the current group have landed
     __syncthreads();     // ... and everybody else's
 
@@ -1149,17 +1196,9 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
       // the stream continues when the previous group (list entry grp - 1, adjacency still in
       // nbrs[nfar]) ran and its centre and i-hi columns of neighbours are this brick's i-lo
       // and centre columns
-      bool cont = false;
-      if constexpr (STREAM) {
-        const unsigned *prv = nbrs + nfar * 36;
-        bool same = true;
-        if (lt < 18) {
-          const int s9 = lt < 9 ? lt : lt - 9, sh = lt < 9 ? 0 : 1;
-          const int base = (s9 / 3) * 9 + (s9 % 3) * 3;  // (dk, dj) = (s9 / 3 - 1, s9 % 3 - 1), di = -1
-          same = nbr[base + sh] == prv[base + sh + 1];
-        }
-        cont = __all_sync(0xFFFFFFFFu, same) && it > 0 && prv[27] != 0 && active;
-      }
+      // (the same test the gather of this group was issued with: its skipped columns are the
+      // ones a continued stream does not read)
+      const bool cont = STREAM && it > 0 && continues(nfar, ncur);
       if (active) {
         T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
         const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);

@@ -361,6 +361,16 @@ typedef struct bk_batch_domain {
   const unsigned *pairs; /* host: ghost plan, npairs (dst, src) brick pairs */
   unsigned npairs;
   int stencil;           /* index into the batch's stencil array */
+  /* Domains whose cell counts are not whole bricks (e.g. 40 cells on 16-wide bricks): n holds
+   * the domain's cells (k, j, i), the brick grid covers them rounded up to whole bricks plus
+   * one ghost brick per side, and grid (host, gdims (k, j, i) bricks, position (k*gj + j)*gi + i
+   * -> brick) locates every cell.  Before every step a cell-level wrap fill writes each cell
+   * within the stencil radius outside the domain with the value at its periodic image; cells
+   * of partial bricks past n are computed by the sweep but belong to no domain.  n = {0,0,0}:
+   * whole bricks (periodic wrap through the adjacency or the ghost plan, as above). */
+  long n[3];
+  long gdims[3];
+  const unsigned *grid;
 } bk_batch_domain;
 
 typedef struct bk_batch bk_batch;
@@ -378,10 +388,14 @@ int bk_batch_create(bk_batch **batch, const bk_batch_domain *doms, unsigned ndom
  * the autotuner's block-count knob. */
 int bk_batch_set_grid(bk_batch *batch, int max_ctas);
 /* Advance every domain `steps` steps: before every `fill_every`-th step (0 = never) the ghost
- * plans are applied to the current input fields, then one launch per stencil sweeps that
- * stencil's segment of the work list.  With use_graph the sequence is captured once per
+ * plans and the wrap fill of partial-brick domains are applied to the current input fields,
+ * then one launch per stencil sweeps that stencil's segment of the work list.  With use_graph the sequence is captured once per
  * (steps, fill_every, parity) into a CUDA graph kept by the batch and replayed on later calls. */
 int bk_batch_run(bk_batch *batch, int steps, int fill_every, int use_graph, void *stream);
+/* on (default): the stencil segments of a step run as parallel branches (one stream each,
+ * joined before the next step), so one segment's last wave overlaps the others' work; 0: one
+ * after another on the caller's stream.  Drops the batch's captured graphs. */
+int bk_batch_set_concurrent(bk_batch *batch, int on);
 /* Which field (0 or 1) holds the newest values. */
 int bk_batch_parity(const bk_batch *batch);
 /* 1 when the batch's domains are brick ranges of one storage (a common brick step, ranges

@@ -196,3 +196,70 @@ def test_batch_rejects_bad_domains():
     st = _abi.lib().bk_batch_create(C.byref(h), C.byref(d), 1, sts, 1, C.byref(B.Layout().to_c()), BK_F32, 0)
     assert st == _abi.BK_ERR_ARG
     assert b"malformed" in _abi.lib().bk_last_error()
+
+
+def _oracle_steps(spec, st, steps, init_cells):
+    """The oracle's periodic array steps (FP64) of one domain from its initial cells."""
+    n = spec.n
+    odom = oracle.Domain(n)
+    o = odom.ghost + odom.pad
+    a = np.zeros(odom.adims)
+    a[o:o + n[0], o:o + n[1], o:o + n[2]] = init_cells
+    bb = np.zeros_like(a)
+    for _ in range(steps):
+        oracle.array_periodic_fill(a, (o,) * 3, n, (8, 8, 8))
+        oracle.array_sweep(a, bb, (o,) * 3, tuple(o + x for x in n), st.offsets(), st.coeff)
+        a, bb = bb, a
+    return a[o:o + n[0], o:o + n[1], o:o + n[2]]
+
+
+@pytest.mark.parametrize("bdim,fold", [((16, 8, 8), (1, 4, 8)), ((8, 8, 32), (1, 1, 32)), ((8, 8, 32), (1, 4, 8))],
+                         ids=["16x8x8", "8x8x32", "8x8x32f48"])
+@pytest.mark.parametrize("arena", [True, False])
+def test_partial_brick_domains_match_the_oracle(bdim, fold, arena):
+    """Domains whose edges are not whole bricks (here multiples of 8 on 16- or 32-wide bricks):
+    padded to whole bricks, periodic through the cell-level wrap fill.  Every domain's cells
+    after 5 FP64 steps equal the oracle's periodic array steps at 1e-12 (mixed test), in arena
+    and per-storage batches, with the segments as parallel branches and one after another."""
+    w = BT.Workload([BT.DomainSpec((24, 40, 16), 0, 11), BT.DomainSpec((40, 24, 56), 1, 12),
+                     BT.DomainSpec((56, 16, 24), 2, 13), BT.DomainSpec((32, 32, 40), 3, 14),
+                     BT.DomainSpec((16, 16, 32), 0, 15)],
+                    [stencils.make(s, 21) for s in BT.BATCH_SHAPES])
+    lay = B.Layout(bdim, fold)
+    assert BT.layout_valid(w, lay)
+    steps = 5
+    for conc in (1, 0):
+        b = BT.Batch(w, lay, BK_F64, arena=arena)
+        assert sum(ds.partial for ds in b.doms) >= 3
+        init = [ds.cells(0).copy() for ds in b.doms]
+        _abi_call("bk_batch_set_concurrent", b.h, conc)
+        b.run(steps, use_graph=bool(conc))
+        B.synchronize()
+        assert B.error_flags() == 0
+        for d, (spec, ds) in enumerate(zip(w.domains, b.doms)):
+            got = ds.cells(b.parity)
+            want = _oracle_steps(spec, w.stencils[spec.stencil], steps, init[d])
+            diff = np.abs(got - want)
+            ok = (diff < 1e-12) | (diff < (np.abs(got) + np.abs(want)) * 1e-12)
+            assert ok.all(), (d, conc, float(diff.max()))
+        b.close()
+
+
+def test_partial_brick_fp32_batch_within_1e5_of_fp64():
+    """The FP32 batch of partial-brick domains against the FP64 batch: normwise 1e-5 per domain."""
+    w = BT.make_workload(ndom=12, seed=5, lo=16, hi=64, multiple=8)
+    lay = B.Layout((16, 8, 8), (1, 4, 8))
+    b32, b64 = BT.Batch(w, lay, BK_F32), BT.Batch(w, lay, BK_F64)
+    b32.run(10)
+    b64.run(10)
+    B.synchronize()
+    for d32, d64 in zip(b32.doms, b64.doms):
+        a, r = d32.cells(b32.parity).astype(np.float64), d64.cells(b64.parity)
+        assert np.abs(a - r).max() <= 1e-5 * np.abs(r).max()
+    b32.close()
+    b64.close()
+
+
+def _abi_call(name, *args):
+    from bricklib_gb300._abi import call
+    call(name, *args)
