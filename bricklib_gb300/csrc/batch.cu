@@ -270,10 +270,9 @@ int batch_dispatch(const BatchStencil &bs, const BatchDomain *doms, unsigned ndo
   if (p.shape == 0) { BK_BSET(8, 8, 8) }
   if constexpr (ACC == ACCM_NATIVE) {
     if (p.shape == 1) { BK_BSET(4, 4, 4) }
-    if constexpr (sizeof(T) == 4) {
-      if (p.shape == 2) { BK_BSET(16, 8, 8) }
-      if (p.shape == 3) { BK_BSET(8, 8, 32) }
-    }
+    // FP32 and FP64: the brick dims the autotuner tries, with folds that are not row-major too
+    if (p.shape == 2) { BK_BSET(16, 8, 8) }
+    if (p.shape == 3) { BK_BSET(8, 8, 32) }
   }
 #undef BK_BSET
 #undef BK_BC
