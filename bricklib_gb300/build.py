@@ -39,11 +39,28 @@ def _deps_mtime() -> float:
     return max((os.path.getmtime(h) for h in hdrs), default=0.0)
 
 
-def _compile(src: str, verbose: bool) -> str:
+def _extra_flags() -> list:
+    """BK_NVCC_FLAGS: extra nvcc flags for experiments with the kernels' build-time switches
+    (e.g. -DBK_CS_SWZ=0); a change of them rebuilds every translation unit."""
+    return os.environ.get("BK_NVCC_FLAGS", "").split()
+
+
+def _flags_changed() -> bool:
+    stamp = os.path.join(BUILD, "flags.txt")
+    want = " ".join(_extra_flags())
+    have = open(stamp).read() if os.path.exists(stamp) else ""
+    if have != want:
+        with open(stamp, "w") as f:
+            f.write(want)
+        return True
+    return False
+
+
+def _compile(src: str, verbose: bool, force: bool = False) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _deps_mtime()):
+    if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _deps_mtime()):
         return obj
-    cmd = [nvcc()] + ARCH + CFLAGS + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + CFLAGS + _extra_flags() + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -57,8 +74,9 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
+    force = _flags_changed()
     with cf.ThreadPoolExecutor(jobs) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+        objs = list(ex.map(lambda s: _compile(s, verbose, force), srcs))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         if verbose:

@@ -88,6 +88,12 @@ __host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, in
   return need;
 }
 
+// 16-element FP32 tile rows with XOR-permuted 16-byte units for the FP32 class-sum stream (1),
+// or rows padded to 20 elements (0)
+#ifndef BK_CS_SWZ
+#define BK_CS_SWZ 1
+#endif
+
 // bricks (warps) per CTA of the column-pair cube kernels: one, so that a CTA's barriers wait
 // for no other warp (GB300, FP32 cube125 at 512^3: 191 / 171 GStencil/s with one / two)
 #ifndef BK_PAIR_NB
@@ -117,7 +123,7 @@ struct Sweep2Cfg {
   // (conflict free) with no padding -- a smaller tile, more CTAs per SM.  BF16: rows of 24
   // (two-way within a half warp, which reads half the bytes of the FP32 case)
   static constexpr bool CS4 = IST && ES <= 4;
-  static constexpr bool SWZ = CS4 && ES == 4 && BI + 2 * RP == 16;
+  static constexpr bool SWZ = BK_CS_SWZ && CS4 && ES == 4 && BI + 2 * RP == 16;
   static constexpr int EI = CS4 ? (ES == 4 ? (SWZ ? 16 : 20) : 24)
                           : PERM ? (NEED % 8 <= 4 ? NEED - NEED % 8 + 4 : NEED - NEED % 8 + 12)
                                  : conflict_free_row(NEED, BI, ES, VE);
@@ -152,6 +158,10 @@ struct Sweep2Cfg {
   static constexpr int NB = CS4 ? 1 : PAIR ? PAIR_NB : cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
   static constexpr int NT = TPB * NB;
   static constexpr int SMEM = NB * PER_BRICK;
+  // resident CTAs asked of the register allocator: the native FP32 / BF16 class-sum stream
+  // (one warp per CTA) at <= 170 registers fits three warps per scheduler (12 per SM), which
+  // its shared memory also allows
+  static constexpr int MINB = CS4 && ACC == ACCM_NATIVE ? 12 : 1;
 };
 
 // Tile coordinates (kk, jj, ii) of plan vector g for the star / cube neighbourhood.
@@ -211,13 +221,42 @@ __device__ __forceinline__ void plan_coords(int g, int &kk, int &jj, int &ii) {
   }
 }
 
+// Class-sum streams: a brick that continues a stream reads only the tile columns from ICUT on
+// (the W of the earlier columns come from the previous brick).  Its plan lists first the copies
+// of columns from ICUT on (NS of each row's NEED / VE copies lie wholly before ICUT), then the
+// others, so a continued brick issues a prefix of the plan.
+template <typename C, int R>
+struct StreamPlan {
+  static constexpr int ICUT = C::ES == 8 ? C::RP + R : C::RP + 4;
+  static constexpr int RV = C::NEED / C::VE;               // copies per tile row
+  static constexpr int NS = ICUT / C::VE;                   // of them wholly before ICUT
+  static constexpr int NN = RV - NS;
+  static constexpr int NVN = C::EK * C::EJ * NN;            // copies a continued brick needs
+};
+
 // Packed plan entry: slot (5 bits) | source element offset in the neighbour brick (13 bits)
 // | destination element offset in the tile (14 bits).  All three fit for bricks up to 8192
-// elements and tiles up to 16384 elements (checked on the host).
-template <typename C, int BK, int BJ, int BI, int R, int FAM>
+// elements and tiles up to 16384 elements (checked on the host).  SORD: the stream order above.
+template <typename C, int BK, int BJ, int BI, int R, int FAM, bool SORD = false>
 __device__ __forceinline__ unsigned plan_entry(int g) {
   int kk, jj, ii;
-  plan_coords<C, BK, BJ, BI, R, FAM>(g, kk, jj, ii);
+  if constexpr (SORD) {
+    typedef StreamPlan<C, R> P;
+    static_assert(FAM != FAM_STAR, "streams are for cubes");
+    int row, chunk;
+    if (g < P::NVN) {
+      row = g / P::NN;
+      chunk = P::NS + g % P::NN;
+    } else {
+      row = (g - P::NVN) / P::NS;
+      chunk = (g - P::NVN) % P::NS;
+    }
+    kk = row / C::EJ;
+    jj = row % C::EJ;
+    ii = chunk * C::VE;
+  } else {
+    plan_coords<C, BK, BJ, BI, R, FAM>(g, kk, jj, ii);
+  }
   const int qk = kk < R ? -1 : (kk >= R + BK ? 1 : 0);
   const int qj = jj < R ? -1 : (jj >= R + BJ ? 1 : 0);
   const int qi = ii < C::RP ? -1 : (ii >= C::RP + BI ? 1 : 0);
@@ -521,15 +560,20 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
 __device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
 
 // four consecutive tile elements as two column pairs
-__device__ __forceinline__ void ld_quad(const float *p, float2 &a, float2 &b) {
-  const float4 v = *reinterpret_cast<const float4 *>(p);
-  a = make_float2(v.x, v.y);
-  b = make_float2(v.z, v.w);
+// (one 16-byte / 8-byte shared-memory load each: the address is 16 / 8-byte aligned by the
+// tile layout, stated to the compiler by the vector load itself)
+// (shared-memory byte address sa)
+__device__ __forceinline__ void ld_quad(float *, unsigned sa, float2 &a, float2 &b) {
+  float x, y, z, w;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];\n" : "=f"(x), "=f"(y), "=f"(z), "=f"(w) : "r"(sa));
+  a = make_float2(x, y);
+  b = make_float2(z, w);
 }
-__device__ __forceinline__ void ld_quad(const __nv_bfloat16 *p, float2 &a, float2 &b) {
-  const uint2 u = *reinterpret_cast<const uint2 *>(p);
-  a = make_float2(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u));
-  b = make_float2(__uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u));
+__device__ __forceinline__ void ld_quad(__nv_bfloat16 *, unsigned sa, float2 &a, float2 &b) {
+  unsigned ux, uy;
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];\n" : "=r"(ux), "=r"(uy) : "r"(sa));
+  a = make_float2(__uint_as_float(ux << 16), __uint_as_float(ux & 0xFFFF0000u));
+  b = make_float2(__uint_as_float(uy << 16), __uint_as_float(uy & 0xFFFF0000u));
 }
 __device__ __forceinline__ void st_elem(float *p, float v) { *p = v; }
 __device__ __forceinline__ void st_elem(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
@@ -556,11 +600,14 @@ __device__ __forceinline__ void cs_group(const T *base, const int j, const int c
                                          float2 (&W)[2][R + 1][2], float2 (&E)[COMP ? 2 : 1][R + 1][2]) {
   constexpr int SK = C::EJ * C::EI, SJ = C::EI;
   float2 Q[2][R + 1][R + 1][2];  // [o][c][b][pair]
+  const unsigned sb = smem_u32(base);
 #pragma unroll
   for (int q = 0; q < 2 * R + 2; ++q) {  // tile plane k0 + q: brick-local plane k0 - R + q
     float2 v[2 * R + 1][2];
 #pragma unroll
-    for (int rr = 0; rr <= 2 * R; ++rr) ld_quad(base + q * SK + rr * SJ + C::col(j + rr, c0), v[rr][0], v[rr][1]);
+    for (int rr = 0; rr <= 2 * R; ++rr)
+      ld_quad((T *)nullptr, sb + (unsigned)((q * SK + rr * SJ + C::col(j + rr, c0)) * (int)sizeof(T)), v[rr][0],
+              v[rr][1]);
     float2 H[R + 1][2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -989,7 +1036,8 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
 // IST: FP64 mirror-symmetric cubes streamed along i (sym_cube_istream): each CTA takes a
 // contiguous share of the list instead of every gridDim.x-th group.
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool BATCH, bool IST>
-__global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST>::NT)
+__global__ void __launch_bounds__(Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST>::NT,
+                                  Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST>::MINB)
 sweep2_kernel(const SweepArgs a, const Taps tp) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC, IST> C;
   constexpr int TPB = C::TPB, NB = C::NB, EPT = C::EPT;
@@ -1015,7 +1063,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
 #pragma unroll
   for (int e = 0; e < EPT; ++e) {
     const int g = e * TPB + lt;
-    plan[e] = g < C::NV ? plan_entry<C, BK, BJ, BI, R, FAM>(g) : 0xFFFFFFFFu;
+    plan[e] = g < C::NV ? plan_entry<C, BK, BJ, BI, R, FAM, IST>(g) : 0xFFFFFFFFu;
   }
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
@@ -1035,10 +1083,15 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     CH = (ngroups + G * rounds - 1) / (G * rounds);
     if (CH < 1) CH = 1;
   }
-  auto next_group = [&](long long g) -> long long {
-    if constexpr (CHUNKED) return ((g + 1) % CH) ? g + 1 : g + 1 + (G - 1) * CH;
-    else if constexpr (STREAM) return g + 1;
-    else return g + G;
+  // a position in this CTA's walk: the group and, chunked, its place in its chunk
+  struct Walk {
+    long long g;
+    long long pos;
+  };
+  auto advance = [&](Walk w) -> Walk {
+    if constexpr (CHUNKED) return w.pos + 1 < CH ? Walk{w.g + 1, w.pos + 1} : Walk{w.g + 1 + (G - 1) * CH, 0};
+    else if constexpr (STREAM) return Walk{w.g + 1, 0};
+    else return Walk{w.g + G, 0};
   };
   const long long g0 = CHUNKED ? (long long)blockIdx.x * CH
                        : STREAM ? (long long)blockIdx.x * ngroups / G : (long long)blockIdx.x;
@@ -1137,7 +1190,8 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   // issue the asynchronous gather of the group staged in nbrs[ns] into raw buffer buf; a
   // continued stream reads only the tile columns from ICUT on (the W of the columns before
   // come from the previous brick), so copies wholly before ICUT are skipped
-  constexpr int ICUT = !STREAM ? 0 : C::ES == 8 ? C::RP + R : C::RP + 4;
+  // plan entries a continued brick issues: those of the first NVN copies (warp-uniform bound)
+  constexpr int EPTN = STREAM ? (StreamPlan<C, R>::NVN + TPB - 1) / TPB : EPT;
   auto issue = [&](int buf, int ns, bool cont) {
     const unsigned *nbr = nbrs + (ns * NB + slot) * 36;
     if (nbr[27]) {
@@ -1145,12 +1199,13 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
       const unsigned tbase = smem_u32(tile);
       const T *in = reinterpret_cast<const T *>(*reinterpret_cast<const unsigned long long *>(nbr + 28));
       const size_t step = *reinterpret_cast<const unsigned long long *>(nbr + 32);
+      const int ne = STREAM && cont ? EPTN : EPT;
 #pragma unroll
       for (int e = 0; e < EPT; ++e) {
         const unsigned p = plan[e];
-        if (p != 0xFFFFFFFFu) {
+        const bool need = !(STREAM && cont) || e * TPB + lt < StreamPlan<C, R>::NVN;
+        if (e < ne && need && p != 0xFFFFFFFFu) {
           const unsigned sl = p & 31u, src = (p >> 5) & 8191u, dst = p >> 18;
-          if (STREAM && cont && C::col((int)(dst / C::EI) % C::EJ, (int)(dst % C::EI)) + C::VE <= ICUT) continue;
           const T *g = in + (size_t)nbr[sl] * step + src;
           cp_async<C::VB>(tbase + dst * C::ES, g);
         }
@@ -1160,10 +1215,12 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   };
 
   // prologue: adjacency of the first two groups, copies of the first
+  Walk w1{g0, 0};
+  Walk w2 = advance(w1), w3 = advance(w2);  // the next group and the one after
   long long grp = g0;
   fetch_adj(grp);
   store_adj(0);
-  fetch_adj(next_group(grp));
+  fetch_adj(w2.g);
   store_adj(1);
   __syncthreads();
   issue(0, 0, false);
@@ -1173,12 +1230,12 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   double W[IST && C::ES == 8 ? 2 : 1][IST && C::ES == 8 ? R + 1 : 1][IST && C::ES == 8 ? 2 * R + 1 : 1];
   CsWin<R, ACC == ACCM_COMP> S4;
 
-  for (int it = 0; grp < gend; grp = next_group(grp), ++it) {
+  for (int it = 0; grp < gend; grp = w2.g, w2 = w3, w3 = advance(w3), ++it) {
     const int cur = it & 1, nxt = cur ^ 1;
     const int ncur = it % 3, nnxt = (it + 1) % 3, nfar = (it + 2) % 3;
     __syncthreads();     // nbrs[nnxt] visible; every thread is done with raw[nxt] and nbrs[nfar]
     issue(nxt, nnxt, STREAM && continues(ncur, nnxt));
-    fetch_adj(next_group(next_group(grp)));  // lands while this group computes
+    fetch_adj(w3.g);  // lands while this group computes
     cp_async_wait<1>();  // this thread's copies for the current group have landed
     __syncthreads();     // ... and everybody else's
 
