@@ -161,7 +161,7 @@ struct Sweep2Cfg {
   // resident CTAs asked of the register allocator: the native FP32 / BF16 class-sum stream
   // (one warp per CTA) at <= 170 registers fits three warps per scheduler (12 per SM), which
   // its shared memory also allows
-  static constexpr int MINB = CS4 && ACC == ACCM_NATIVE ? 12 : 1;
+  static constexpr int MINB = CS4 && ACC == ACCM_NATIVE ? 12 : 0;
 };
 
 // Tile coordinates (kk, jj, ii) of plan vector g for the star / cube neighbourhood.
