@@ -575,8 +575,18 @@ __device__ __forceinline__ void ld_quad(__nv_bfloat16 *, unsigned sa, float2 &a,
   a = make_float2(__uint_as_float(ux << 16), __uint_as_float(ux & 0xFFFF0000u));
   b = make_float2(__uint_as_float(uy << 16), __uint_as_float(uy & 0xFFFF0000u));
 }
-__device__ __forceinline__ void st_elem(float *p, float v) { *p = v; }
-__device__ __forceinline__ void st_elem(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+// four consecutive parked outputs -> tile: one 16-byte (FP32) / 8-byte (BF16) shared store at
+// shared-memory byte address sa (aligned by the tile layout)
+__device__ __forceinline__ void sts_quad(float *, unsigned sa, const float (&v)[4]) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(sa), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
+               : "memory");
+}
+__device__ __forceinline__ void sts_quad(__nv_bfloat16 *, unsigned sa, const float (&v)[4]) {
+  const __nv_bfloat162 lo = __floats2bfloat162_rn(v[0], v[1]), hi = __floats2bfloat162_rn(v[2], v[3]);
+  asm volatile("st.shared.v2.u32 [%0], {%1, %2};\n" ::"r"(sa), "r"(*reinterpret_cast<const unsigned *>(&lo)),
+               "r"(*reinterpret_cast<const unsigned *>(&hi))
+               : "memory");
+}
 // four parked outputs (tile) -> global memory: one 16-byte (FP32) / 8-byte (BF16) store
 __device__ __forceinline__ void st_quad(float *g, const float *t) {
   __stcs(reinterpret_cast<float4 *>(g), *reinterpret_cast<const float4 *>(t));
@@ -683,13 +693,18 @@ __device__ __forceinline__ float cs_at(const float2 (&P)[NO][R + 1][2], const fl
 }
 
 // Outputs of the current group's four columns c0 .. c0 + 3 for both rows, parked in the tile at
-// their own input positions (park: tile row prow = j + R of plane k0 + R).
+// their own input positions (park: tile row prow = j + R of plane k0 + R), one vector store per
+// row (the four columns are one 16-byte unit of the row, also under the FP32 swizzle; the eight
+// lanes of a quarter warp hit distinct banks).
 template <typename C, typename T, int R, bool COMP>
 __device__ __forceinline__ void cs_out(T *park, const int prow, const int c0, const CsWin<R, COMP> &S,
                                        const float2 (&Wn)[2][R + 1][2], const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
   constexpr int SK = C::EJ * C::EI;
+  static_assert(C::SWZ || C::EI % 4 == 0, "four parked columns stay in one aligned unit");
+  const unsigned pb = smem_u32(park + C::col(prow, c0));
 #pragma unroll
-  for (int o = 0; o < 2; ++o)
+  for (int o = 0; o < 2; ++o) {
+    float q[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       float v;
@@ -708,8 +723,10 @@ __device__ __forceinline__ void cs_out(T *park, const int prow, const int c0, co
         }
         v = sm + (cm + es);
       }
-      st_elem(park + o * SK + C::col(prow, c0 + t), v);
+      q[t] = v;
     }
+    sts_quad((T *)nullptr, pb + (unsigned)(o * SK * (int)sizeof(T)), q);
+  }
 }
 
 template <int R, bool COMP>
