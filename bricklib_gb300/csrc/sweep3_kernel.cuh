@@ -56,8 +56,11 @@ struct StarTmaCfg {
                        O_JH = O_JL + al(B_JF), O_IL = O_JH + al(B_JF), O_IH = O_IL + al(B_IF);
   static constexpr int BRICK = O_IH + al(B_IF);               // bytes of one brick's stage buffer
   static constexpr int TX = B_C + 2 * (B_KF + B_JF + B_IF);  // bytes the copies of one brick deliver
-  // after the stage buffers: full[4], empty[4] mbarriers, centre brick index [4][NB], abort word
-  static constexpr int META = 64 + 4 * TMA_MAX_STAGES * NB + 16;
+  // after the stage buffers: full[4], empty[4] mbarriers, centre brick index [4][NB], abort word,
+  // the FP64 coefficients (NTAP doubles, 8-byte aligned)
+  static constexpr int NTAP = 1 + 6 * R;
+  static constexpr int O_COEF = 64 + 4 * TMA_MAX_STAGES * NB + 16;
+  static constexpr int META = O_COEF + 8 * NTAP;
   static constexpr int smem(int stages) { return 128 + stages * NB * BRICK + META; }  // + base alignment slack
 };
 
@@ -271,6 +274,43 @@ __device__ __forceinline__ void star_column(const unsigned char *buf, const int 
   }
 }
 
+// The native FP64 column: the same operations in the same order per point as star_column, with
+// the coefficients in registers (cr, read from shared memory once per thread) and the loop over
+// the column's BK points innermost, so that consecutive multiply-adds share one coefficient and
+// each takes its other factor straight from a shared-memory load.  On GB300 the FP64 pipe runs
+// about a fifth slower when a multiply-add reads its coefficient from the constant bank (measured
+// with a standalone probe: 1.01 against 1.20 TFLOP/s with shared-memory operands).
+template <int BK, int BJ, int BI, int R>
+__device__ __forceinline__ void star_column_f64(const unsigned char *buf, const int cKL, const int cC, const int cKH,
+                                                const int (&oi)[2 * R], const int (&si)[2 * R], const int (&oj)[2 * R],
+                                                const int (&sj)[2 * R], double *ob, const double (&cr)[1 + 6 * R]) {
+  constexpr int PK = BJ * BI;
+  const double *f = reinterpret_cast<const double *>(buf);
+  // plane kk in [-R, BK + R) of this column: k-lo face, centre or k-hi face
+  auto kv = [&](int kk) { return kk < 0 ? f[cKL + (kk + R) * PK] : kk >= BK ? f[cKH + (kk - BK) * PK] : f[cC + kk * PK]; };
+  double acc[BK];
+#pragma unroll
+  for (int k = 0; k < BK; ++k) acc[k] = cr[0] * kv(k);
+#pragma unroll
+  for (int d = 1; d <= R; ++d) {
+    const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + 0], f[oi[q] + k * si[q]], acc[k]);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + 1], f[oi[q + 1] + k * si[q + 1]], acc[k]);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + 2], f[oj[q] + k * sj[q]], acc[k]);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + 3], f[oj[q + 1] + k * sj[q + 1]], acc[k]);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + 4], kv(k + d), acc[k]);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + 5], kv(k - d), acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < BK; ++k) store_stream(ob + k * PK, acc[k]);
+}
+
 template <typename T, int BK, int BJ, int BI, int R, int ACC, bool NI>
 __global__ void __launch_bounds__(StarTmaCfg<T, BK, BJ, BI, R, NI>::NT)
 sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, const Taps tp, const int S) {
@@ -299,6 +339,9 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     fence_proxy_async_smem();
   }
+  static_assert(C::NT >= C::NTAP, "one thread per coefficient");
+  double *coef_s = reinterpret_cast<double *>(sm + S * NB * C::BRICK + C::O_COEF);
+  if (threadIdx.x < C::NTAP) coef_s[threadIdx.x] = tp.c[threadIdx.x];
   __syncthreads();
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
@@ -422,6 +465,11 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     }
   }
 
+  constexpr bool F64R = ACC == ACCM_NATIVE && C::ES == 8;  // FP64 column with register coefficients
+  double cr[C::NTAP];
+#pragma unroll
+  for (int t = 0; t < C::NTAP; ++t) cr[t] = F64R ? coef_s[t] : 0.0;
+
   int st = 0;
   unsigned ph = 0;  // phase parity of the stage's current use
   for (long long g = g0; g < ngroups; g += gstep) {
@@ -447,8 +495,12 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     }
     if (active) {
       T *ob = reinterpret_cast<T *>(a.out) + a.out_off + (size_t)ob_idx * a.out_step + (size_t)(j * BI + i);
-      star_column<T, BK, BJ, BI, R, ACC>(buf, eKL + j * BI + i, eC + j * BI + i, eKH + j * BI + i, oi, si, oj, sj, ob,
-                                         tp);
+      if constexpr (F64R)
+        star_column_f64<BK, BJ, BI, R>(buf, eKL + j * BI + i, eC + j * BI + i, eKH + j * BI + i, oi, si, oj, sj,
+                                       reinterpret_cast<double *>(ob), cr);
+      else
+        star_column<T, BK, BJ, BI, R, ACC>(buf, eKL + j * BI + i, eC + j * BI + i, eKH + j * BI + i, oi, si, oj, sj,
+                                           ob, tp);
     }
     // the float-float conversion wrote the stage through the generic proxy; order those
     // writes before the copies that refill it
