@@ -38,6 +38,22 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// FP64 arithmetic on register operands only.  On GB300 a DADD, a DMUL, or a DFMA that reads its
+// coefficient from the constant bank issues about a fifth slower than a DFMA whose operands are
+// all registers (standalone probe, 16 warps per SM: 0.80 against 0.955 of the DFMA rate), so the
+// native FP64 kernels write a + b as fma(1, a, b) and c * x as fma(c, x, -0), with 1 and -0 in
+// registers, and read their coefficients from shared memory into registers.  The bits are those
+// of the plain operations: 1 * a is exact and -0 is the identity of every sum (signed zeros
+// included), so each form rounds once, as the plain operation does.  The shared-memory block
+// (F64Ops::NHEAD doubles, then the coefficients) is filled from Taps::one / mzero / c.
+struct F64Ops {
+  static constexpr int NHEAD = 2;
+  double one, mz;
+  __device__ __forceinline__ static F64Ops load(const double *cs) { return F64Ops{cs[0], cs[1]}; }
+  __device__ __forceinline__ double add(double a, double b) const { return fma(one, a, b); }
+  __device__ __forceinline__ double mul(double c, double x) const { return fma(c, x, mz); }
+};
+
 __device__ __forceinline__ void store_stream(double *p, double v) { __stcs(p, v); }
 __device__ __forceinline__ void store_stream(float *p, float v) { __stcs(p, v); }
 __device__ __forceinline__ void store_stream(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
@@ -157,7 +173,18 @@ struct Sweep2Cfg {
   static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 36 * 4;
   static constexpr int NB = CS4 ? 1 : PAIR ? PAIR_NB : cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
   static constexpr int NT = TPB * NB;
-  static constexpr int SMEM = NB * PER_BRICK;
+  // native FP64: the register-operand block (F64Ops head, then the coefficients the family reads:
+  // star taps, cube taps, or the symmetry classes, Taps::c from CBASE on) after the tiles and the
+  // adjacency slots
+  static constexpr bool F64R = ES == 8 && ACC == ACCM_NATIVE;
+  static constexpr bool SYMF = FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ;
+  static constexpr int NCOEF = FAM == FAM_STAR ? 1 + 6 * R
+                             : FAM == FAM_CUBE ? (2 * R + 1) * (2 * R + 1) * (2 * R + 1)
+                             : SYMF ? (R + 1) * (R + 1) * (R + 1) : 0;
+  static constexpr int CBASE = SYMF ? sym_index(0, 0, 0, R) : 0;
+  static_assert(!SYMF || sym_index(R, R, R, R) - CBASE + 1 == NCOEF, "the class block holds every class");
+  static constexpr int COEFB = F64R ? ((F64Ops::NHEAD + NCOEF) * 8 + 15) / 16 * 16 : 0;
+  static constexpr int SMEM = NB * PER_BRICK + COEFB;
   // resident CTAs asked of the register allocator: the native FP32 / BF16 class-sum stream
   // (one warp per CTA) at <= 170 registers fits three warps per scheduler (12 per SM), which
   // its shared memory also allows
@@ -465,11 +492,21 @@ __device__ __forceinline__ void sym_cube_pair_shared(const T *rt, T *ob, const i
 // warp), and the finished brick leaves in whole-warp 512-byte stores, which also suits an
 // output field in mapped host memory.
 template <typename C, int R, bool KJ>
-__device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const int lane, const Taps &tp,
+__device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const int lane, const double *cs,
                                                  double (&W)[2][R + 1][2 * R + 1], const bool cont) {
   constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP, NW = 2 * R + 1;
   static_assert(R == 1 || R == 2, "cube radius");
   const int k0 = 2 * (lane >> 3), j = lane & 7;
+  // register operands (F64Ops): the class coefficients coef(c, b, a), 1 and -0
+  static_assert(C::F64R && C::SYMF, "native FP64 classes");
+  const F64Ops f = F64Ops::load(cs);
+  double cf[R + 1][R + 1][R + 1];
+#pragma unroll
+  for (int c = 0; c <= R; ++c)
+#pragma unroll
+    for (int b = 0; b <= R; ++b)
+#pragma unroll
+      for (int a = 0; a <= R; ++a) cf[c][b][a] = cs[F64Ops::NHEAD + sym_index(c, b, a, R) - C::CBASE];
   double *col = rt + (k0 + R) * SK + (j + R) * SJ;  // tile row of brick-local (k0, j), column 0
   // W_a of tile column ii for both rows, pushed into the window (newest at NW - 1)
   auto column = [&](const int ii) {
@@ -479,7 +516,7 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
       const double *p = col + (q - R) * SK + ii;
       H[0][q] = p[0];
 #pragma unroll
-      for (int b = 1; b <= R; ++b) H[b][q] = p[-b * SJ] + p[b * SJ];
+      for (int b = 1; b <= R; ++b) H[b][q] = f.add(p[-b * SJ], p[b * SJ]);
     }
 #pragma unroll
     for (int o = 0; o < 2; ++o) {
@@ -488,13 +525,13 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
       for (int b = 0; b <= R; ++b) {
         Q[0][b] = H[b][R + o];
 #pragma unroll
-        for (int c = 1; c <= R; ++c) Q[c][b] = H[b][R + o - c] + H[b][R + o + c];
+        for (int c = 1; c <= R; ++c) Q[c][b] = f.add(H[b][R + o - c], H[b][R + o + c]);
       }
       if constexpr (KJ) {
 #pragma unroll
         for (int c = 1; c <= R; ++c)
 #pragma unroll
-          for (int b = 0; b < c; ++b) Q[c][b] += Q[b][c];
+          for (int b = 0; b < c; ++b) Q[c][b] = f.add(Q[c][b], Q[b][c]);
       }
 #pragma unroll
       for (int a = 0; a <= R; ++a) {
@@ -502,10 +539,8 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
 #pragma unroll
         for (int c = 0; c <= R; ++c)
 #pragma unroll
-          for (int b = 0; b <= (KJ ? c : R); ++b) {
-            const double cf = tp.c[sym_index(c, b, a, R)];
-            w = (c == 0 && b == 0) ? cf * Q[0][0] : fma(cf, Q[c][b], w);
-          }
+          for (int b = 0; b <= (KJ ? c : R); ++b)
+            w = (c == 0 && b == 0) ? f.mul(cf[0][0][a], Q[0][0]) : fma(cf[c][b][a], Q[c][b], w);
 #pragma unroll
         for (int m = 0; m + 1 < NW; ++m) W[o][a][m] = W[o][a][m + 1];
         W[o][a][NW - 1] = w;
@@ -524,7 +559,7 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
     for (int o = 0; o < 2; ++o) {
       double v = W[o][0][R];
 #pragma unroll
-      for (int a = 1; a <= R; ++a) v += W[o][a][R - a] + W[o][a][R + a];
+      for (int a = 1; a <= R; ++a) v = f.add(v, f.add(W[o][a][R - a], W[o][a][R + a]));
       col[o * SK + RP + i] = v;
     }
   }
@@ -792,8 +827,9 @@ __device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, 
 // threads (lt) owns one (j, i) column, or, for the column-pair cubes, each of the BJ*BI/2
 // threads a pair of columns.
 // out_brick: the output field's brick (field base + centre brick x step).
+// cs: the native FP64 register-operand block (F64Ops) in shared memory.
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
-__device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, const Taps &tp) {
+__device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, const Taps &tp, const double *cs) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
   typedef typename Elem<T>::acc AT;
   constexpr int EJ = C::EJ, EI = C::EI, SK = EJ * EI, SJ = EI, RP = C::RP;
@@ -907,6 +943,51 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
         store_stream(ob + k * BJ * BI, acc.result());
       }
     }
+  } else if constexpr (C::F64R && FAM == FAM_STAR) {
+    // the per-point operations of the star below, taps outer over the column's points, on
+    // register operands (F64Ops), every multiply-add with its value freshly loaded
+    const F64Ops f = F64Ops::load(cs);
+    double cr[1 + 6 * R];
+#pragma unroll
+    for (int t = 0; t < 1 + 6 * R; ++t) cr[t] = cs[F64Ops::NHEAD + t];
+    const double *c0 = reinterpret_cast<const double *>(rt) + R * SK + cofs;  // point k at c0[k * SK]
+    double acc[BK];
+#pragma unroll
+    for (int k = 0; k < BK; ++k) acc[k] = f.mul(cr[0], c0[k * SK]);
+#pragma unroll
+    for (int d = 1; d <= R; ++d) {
+      const int t = 1 + 6 * (d - 1);
+      const int off[6] = {d, -d, d * SJ, -d * SJ, d * SK, -d * SK};
+#pragma unroll
+      for (int q = 0; q < 6; ++q)
+#pragma unroll
+        for (int k = 0; k < BK; ++k) acc[k] = fma(cr[t + q], c0[k * SK + off[q]], acc[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < BK; ++k) store_stream(reinterpret_cast<double *>(ob) + k * BJ * BI, acc[k]);
+  } else if constexpr (C::F64R && FAM == FAM_CUBE) {
+    // the per-point operations of the cube below ((dj, di) outer, dk inner), taps outer over the
+    // column's points, on register operands (F64Ops), every multiply-add with its value freshly
+    // loaded
+    const F64Ops f = F64Ops::load(cs);
+    const double *c0 = reinterpret_cast<const double *>(rt) + cofs;  // plane kk at c0[kk * SK]
+    double acc[BK];
+#pragma unroll
+    for (int dj = -R; dj <= R; ++dj)
+#pragma unroll
+      for (int di = -R; di <= R; ++di)
+#pragma unroll
+        for (int dk = -R; dk <= R; ++dk) {
+          const int t = ((dk + R) * (2 * R + 1) + (dj + R)) * (2 * R + 1) + (di + R);
+          const double cf = cs[F64Ops::NHEAD + t];
+#pragma unroll
+          for (int k = 0; k < BK; ++k) {
+            const double x = c0[(k + R + dk) * SK + dj * SJ + di];
+            acc[k] = (dj == -R && di == -R && dk == -R) ? f.mul(cf, x) : fma(cf, x, acc[k]);
+          }
+        }
+#pragma unroll
+    for (int k = 0; k < BK; ++k) store_stream(reinterpret_cast<double *>(ob) + k * BJ * BI, acc[k]);
   } else {
     if constexpr (FAM == FAM_STAR) {
       AT w[BK + 2 * R];
@@ -1231,6 +1312,14 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     cp_async_commit();
   };
 
+  // native FP64: the register-operand block (F64Ops), read after the prologue's barrier
+  const double *cs = reinterpret_cast<const double *>(smem_raw + NB * C::PER_BRICK);
+  if constexpr (C::F64R) {
+    double *csw = reinterpret_cast<double *>(smem_raw + NB * C::PER_BRICK);
+    for (int e = threadIdx.x; e < F64Ops::NHEAD + C::NCOEF; e += C::NT)
+      csw[e] = e == 0 ? tp.one : e == 1 ? tp.mzero : tp.c[C::CBASE + e - F64Ops::NHEAD];
+  }
+
   // prologue: adjacency of the first two groups, copies of the first
   Walk w1{g0, 0};
   Walk w2 = advance(w1), w3 = advance(w2);  // the next group and the one after
@@ -1279,8 +1368,8 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
         T *ob = out + (size_t)nbr[13] * ostep;
         T *tile = const_cast<T *>(rt);  // this warp's buffer until the next barrier
         if constexpr (C::ES == 8) {
-          if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, tp, W, cont);
-          else sym_cube_istream<C, R, false>(tile, ob, lt, tp, W, cont);
+          if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, cs, W, cont);
+          else sym_cube_istream<C, R, false>(tile, ob, lt, cs, W, cont);
         } else {
           constexpr bool CM = ACC == ACCM_COMP;
           if (tp.kj) sym_cube_istream4<C, T, R, true, CM>(tile, ob, lt, tp, S4, cont);
@@ -1290,7 +1379,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     } else if (active) {
       T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
       const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
-      sweep2_brick<T, BK, BJ, BI, R, FAM, ACC>(rt, out + (size_t)nbr[13] * ostep, lt, tp);
+      sweep2_brick<T, BK, BJ, BI, R, FAM, ACC>(rt, out + (size_t)nbr[13] * ostep, lt, tp, cs);
     }
     store_adj(nfar);  // group it + 2; read after the next iteration's first barrier
   }

@@ -57,10 +57,10 @@ struct StarTmaCfg {
   static constexpr int BRICK = O_IH + al(B_IF);               // bytes of one brick's stage buffer
   static constexpr int TX = B_C + 2 * (B_KF + B_JF + B_IF);  // bytes the copies of one brick deliver
   // after the stage buffers: full[4], empty[4] mbarriers, centre brick index [4][NB], abort word,
-  // the FP64 coefficients (NTAP doubles, 8-byte aligned)
+  // the FP64 register-operand block (F64Ops head, then NTAP coefficients; 8-byte aligned)
   static constexpr int NTAP = 1 + 6 * R;
   static constexpr int O_COEF = 64 + 4 * TMA_MAX_STAGES * NB + 16;
-  static constexpr int META = O_COEF + 8 * NTAP;
+  static constexpr int META = O_COEF + 8 * (F64Ops::NHEAD + NTAP);
   static constexpr int smem(int stages) { return 128 + stages * NB * BRICK + META; }  // + base alignment slack
 };
 
@@ -274,23 +274,22 @@ __device__ __forceinline__ void star_column(const unsigned char *buf, const int 
   }
 }
 
-// The native FP64 column: the same operations in the same order per point as star_column, with
-// the coefficients in registers (cr, read from shared memory once per thread) and the loop over
-// the column's BK points innermost, so that consecutive multiply-adds share one coefficient and
-// each takes its other factor straight from a shared-memory load.  On GB300 the FP64 pipe runs
-// about a fifth slower when a multiply-add reads its coefficient from the constant bank (measured
-// with a standalone probe: 1.01 against 1.20 TFLOP/s with shared-memory operands).
+// The native FP64 column: the same operations in the same order per point as star_column, on
+// register operands only (F64Ops; the coefficients cr read from shared memory once per thread),
+// with the loop over the column's BK points innermost, so that consecutive multiply-adds share
+// one coefficient and each takes its other factor straight from a shared-memory load.
 template <int BK, int BJ, int BI, int R>
 __device__ __forceinline__ void star_column_f64(const unsigned char *buf, const int cKL, const int cC, const int cKH,
                                                 const int (&oi)[2 * R], const int (&si)[2 * R], const int (&oj)[2 * R],
-                                                const int (&sj)[2 * R], double *ob, const double (&cr)[1 + 6 * R]) {
+                                                const int (&sj)[2 * R], double *ob, const double (&cr)[1 + 6 * R],
+                                                const F64Ops &f64) {
   constexpr int PK = BJ * BI;
   const double *f = reinterpret_cast<const double *>(buf);
   // plane kk in [-R, BK + R) of this column: k-lo face, centre or k-hi face
   auto kv = [&](int kk) { return kk < 0 ? f[cKL + (kk + R) * PK] : kk >= BK ? f[cKH + (kk - BK) * PK] : f[cC + kk * PK]; };
   double acc[BK];
 #pragma unroll
-  for (int k = 0; k < BK; ++k) acc[k] = cr[0] * kv(k);
+  for (int k = 0; k < BK; ++k) acc[k] = f64.mul(cr[0], kv(k));
 #pragma unroll
   for (int d = 1; d <= R; ++d) {
     const int t = 1 + 6 * (d - 1), q = 2 * (d - 1);
@@ -339,9 +338,10 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     fence_proxy_async_smem();
   }
-  static_assert(C::NT >= C::NTAP, "one thread per coefficient");
+  static_assert(C::NT >= F64Ops::NHEAD + C::NTAP, "one thread per entry");
   double *coef_s = reinterpret_cast<double *>(sm + S * NB * C::BRICK + C::O_COEF);
-  if (threadIdx.x < C::NTAP) coef_s[threadIdx.x] = tp.c[threadIdx.x];
+  if (threadIdx.x < F64Ops::NHEAD + C::NTAP)
+    coef_s[threadIdx.x] = threadIdx.x == 0 ? tp.one : threadIdx.x == 1 ? tp.mzero : tp.c[threadIdx.x - F64Ops::NHEAD];
   __syncthreads();
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;
@@ -468,7 +468,8 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
   constexpr bool F64R = ACC == ACCM_NATIVE && C::ES == 8;  // FP64 column with register coefficients
   double cr[C::NTAP];
 #pragma unroll
-  for (int t = 0; t < C::NTAP; ++t) cr[t] = F64R ? coef_s[t] : 0.0;
+  for (int t = 0; t < C::NTAP; ++t) cr[t] = F64R ? coef_s[F64Ops::NHEAD + t] : 0.0;
+  const F64Ops f64 = F64R ? F64Ops::load(coef_s) : F64Ops{0.0, 0.0};
 
   int st = 0;
   unsigned ph = 0;  // phase parity of the stage's current use
@@ -497,7 +498,7 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
       T *ob = reinterpret_cast<T *>(a.out) + a.out_off + (size_t)ob_idx * a.out_step + (size_t)(j * BI + i);
       if constexpr (F64R)
         star_column_f64<BK, BJ, BI, R>(buf, eKL + j * BI + i, eC + j * BI + i, eKH + j * BI + i, oi, si, oj, sj,
-                                       reinterpret_cast<double *>(ob), cr);
+                                       reinterpret_cast<double *>(ob), cr, f64);
       else
         star_column<T, BK, BJ, BI, R, ACC>(buf, eKL + j * BI + i, eC + j * BI + i, eKH + j * BI + i, oi, si, oj, sj,
                                            ob, tp);
