@@ -487,10 +487,9 @@ __device__ __forceinline__ void sym_cube_pair_shared(const T *rt, T *ob, const i
 // 125-point cube takes 43 FP64 operations per point, 37 when its coefficients are also
 // symmetric under k <-> j (Q(c, b) + Q(b, c) share one multiply-add).  Each W depends on one
 // input column only, so a brick's outputs are the same bits whether the W of its first 2R
-// columns were carried or computed from its own tile.  Output (k, j, i) is parked in the tile
-// at its own input position, whose column was consumed R steps earlier (the CTA is this one
-// warp), and the finished brick leaves in whole-warp 512-byte stores, which also suits an
-// output field in mapped host memory.
+// columns were carried or computed from its own tile.  A lane keeps the outputs of its two rows
+// in registers and stores them at the end of the brick.  All arithmetic runs on register operands
+// (F64Ops).
 template <typename C, int R, bool KJ>
 __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const int lane, const double *cs,
                                                  double (&W)[2][R + 1][2 * R + 1], const bool cont) {
@@ -551,25 +550,27 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
 #pragma unroll
     for (int ii = RP - R; ii < RP + R; ++ii) column(ii);
   }
+  // the lane's outputs stay in registers: with no shared-memory stores in the column loop the
+  // loads of later columns may issue under the arithmetic of earlier ones
+  double outv[2][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     column(RP + R + i);  // the window now ends at column i + R: output i is complete
-    __syncwarp();        // every lane is past column RP + i
 #pragma unroll
     for (int o = 0; o < 2; ++o) {
       double v = W[o][0][R];
 #pragma unroll
       for (int a = 1; a <= R; ++a) v = f.add(v, f.add(W[o][a][R - a], W[o][a][R + a]));
-      col[o * SK + RP + i] = v;
+      outv[o][i] = v;
     }
   }
-  __syncwarp();
-  // 64 outputs per store: lane l writes elements 2l, 2l + 1 of rows 8q .. 8q + 7
+  // rows (k0, j) and (k0 + 1, j) of the output brick, 16 bytes per store (the eight lanes of a
+  // plane cover 512 contiguous bytes in four stores)
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int e = q * 64 + 2 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
-    st_pair(ob + e, ld_pair(rt + (k + R) * SK + (jj + R) * SJ + RP + i));
-  }
+  for (int o = 0; o < 2; ++o)
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      st_pair(ob + ((k0 + o) * 8 + j) * 8 + 2 * c, make_double2(outv[o][2 * c], outv[o][2 * c + 1]));
 }
 
 // ---------------------------------------------------------------------------------------
