@@ -82,6 +82,8 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   tp->post = st->post_op;
   tp->one = 1.0;
   tp->mzero = -0.0;
+  tp->one_mz[0] = 1.0;
+  tp->one_mz[1] = -0.0;
   static thread_local int offs[BK_MAX_TAPS][3];
   static thread_local int toff1[BK_MAX_TAPS];
   const int EJ = L.bj + 2 * GENERIC_R, EI = L.bi + 2 * GENERIC_R;

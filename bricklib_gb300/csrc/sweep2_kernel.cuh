@@ -44,15 +44,30 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // native FP64 kernels write a + b as fma(1, a, b) and c * x as fma(c, x, -0), with 1 and -0 in
 // registers, and read their coefficients from shared memory into registers.  The bits are those
 // of the plain operations: 1 * a is exact and -0 is the identity of every sum (signed zeros
-// included), so each form rounds once, as the plain operation does.  The shared-memory block
-// (F64Ops::NHEAD doubles, then the coefficients) is filled from Taps::one / mzero / c.
+// included), so each form rounds once, as the plain operation does.  The operands come either
+// from a shared-memory block (F64Ops::NHEAD doubles, then the coefficients, filled from
+// Taps::one / mzero / c) or straight from the kernel parameters at an index that carries a
+// per-thread zero the compiler cannot see through: the loads then land in per-thread registers
+// (a parameter read at a uniform index measured as slow as a constant-bank operand: cube27
+// 19.0 against 22.4 GStencil/s), are neither merged nor hoisted, and cost no shared memory.
+__device__ __forceinline__ int opaque_zero() {
+  int z;
+  asm volatile("mov.u32 %0, 0;\n" : "=r"(z));
+  return z;
+}
 struct F64Ops {
   static constexpr int NHEAD = 2;
   double one, mz;
   __device__ __forceinline__ static F64Ops load(const double *cs) { return F64Ops{cs[0], cs[1]}; }
+  __device__ __forceinline__ static F64Ops load(const Taps &tp) {
+    const int z = opaque_zero();
+    return F64Ops{tp.one_mz[z], tp.one_mz[z + 1]};
+  }
   __device__ __forceinline__ double add(double a, double b) const { return fma(one, a, b); }
   __device__ __forceinline__ double mul(double c, double x) const { return fma(c, x, mz); }
 };
+// coefficient t of Taps::c as a per-thread register operand, loaded at each call
+__device__ __forceinline__ double f64_coef(const Taps &tp, int t) { return tp.c[t + opaque_zero()]; }
 
 __device__ __forceinline__ void store_stream(double *p, double v) { __stcs(p, v); }
 __device__ __forceinline__ void store_stream(float *p, float v) { __stcs(p, v); }
@@ -173,17 +188,15 @@ struct Sweep2Cfg {
   static constexpr int PER_BRICK = 2 * TILE_BYTES + FTILE_BYTES + 3 * 36 * 4;
   static constexpr int NB = CS4 ? 1 : PAIR ? PAIR_NB : cmax(1, cmin(cmax(1, 128 / TPB), (100 * 1024) / PER_BRICK));
   static constexpr int NT = TPB * NB;
-  // native FP64: the register-operand block (F64Ops head, then the coefficients the family reads:
-  // star taps, cube taps, or the symmetry classes, Taps::c from CBASE on) after the tiles and the
-  // adjacency slots
+  // native FP64 arithmetic on register operands (F64Ops).  Stars and cubes read them from a
+  // shared-memory block after the tiles and the adjacency slots (F64Ops head, then the taps'
+  // coefficients); the class-sum streams read them from the kernel parameters (a block would cost
+  // them a resident CTA per SM, and they measured the same either way).
   static constexpr bool F64R = ES == 8 && ACC == ACCM_NATIVE;
   static constexpr bool SYMF = FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ;
-  static constexpr int NCOEF = FAM == FAM_STAR ? 1 + 6 * R
-                             : FAM == FAM_CUBE ? (2 * R + 1) * (2 * R + 1) * (2 * R + 1)
-                             : SYMF ? (R + 1) * (R + 1) * (R + 1) : 0;
-  static constexpr int CBASE = SYMF ? sym_index(0, 0, 0, R) : 0;
-  static_assert(!SYMF || sym_index(R, R, R, R) - CBASE + 1 == NCOEF, "the class block holds every class");
-  static constexpr int COEFB = F64R ? ((F64Ops::NHEAD + NCOEF) * 8 + 15) / 16 * 16 : 0;
+  static constexpr bool F64S = F64R && (FAM == FAM_STAR || FAM == FAM_CUBE);
+  static constexpr int NCOEF = FAM == FAM_STAR ? 1 + 6 * R : (2 * R + 1) * (2 * R + 1) * (2 * R + 1);
+  static constexpr int COEFB = F64S ? ((F64Ops::NHEAD + NCOEF) * 8 + 15) / 16 * 16 : 0;
   static constexpr int SMEM = NB * PER_BRICK + COEFB;
   // resident CTAs asked of the register allocator: the native FP32 / BF16 class-sum stream
   // (one warp per CTA) at <= 170 registers fits three warps per scheduler (12 per SM), which
@@ -487,25 +500,19 @@ __device__ __forceinline__ void sym_cube_pair_shared(const T *rt, T *ob, const i
 // 125-point cube takes 43 FP64 operations per point, 37 when its coefficients are also
 // symmetric under k <-> j (Q(c, b) + Q(b, c) share one multiply-add).  Each W depends on one
 // input column only, so a brick's outputs are the same bits whether the W of its first 2R
-// columns were carried or computed from its own tile.  A lane keeps the outputs of its two rows
-// in registers and stores them at the end of the brick.  All arithmetic runs on register operands
-// (F64Ops).
+// columns were carried or computed from its own tile.  Output (k, j, i) is parked in the tile
+// at its own input position, whose column was consumed R steps earlier (the CTA is this one
+// warp), and the finished brick leaves in whole-warp 512-byte stores.  All arithmetic runs on
+// register operands (F64Ops).
 template <typename C, int R, bool KJ>
-__device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const int lane, const double *cs,
+__device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const int lane, const Taps &tp,
                                                  double (&W)[2][R + 1][2 * R + 1], const bool cont) {
   constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP, NW = 2 * R + 1;
   static_assert(R == 1 || R == 2, "cube radius");
   const int k0 = 2 * (lane >> 3), j = lane & 7;
   // register operands (F64Ops): the class coefficients coef(c, b, a), 1 and -0
   static_assert(C::F64R && C::SYMF, "native FP64 classes");
-  const F64Ops f = F64Ops::load(cs);
-  double cf[R + 1][R + 1][R + 1];
-#pragma unroll
-  for (int c = 0; c <= R; ++c)
-#pragma unroll
-    for (int b = 0; b <= R; ++b)
-#pragma unroll
-      for (int a = 0; a <= R; ++a) cf[c][b][a] = cs[F64Ops::NHEAD + sym_index(c, b, a, R) - C::CBASE];
+  const F64Ops f = F64Ops::load(tp);
   double *col = rt + (k0 + R) * SK + (j + R) * SJ;  // tile row of brick-local (k0, j), column 0
   // W_a of tile column ii for both rows, pushed into the window (newest at NW - 1)
   auto column = [&](const int ii) {
@@ -517,32 +524,40 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
 #pragma unroll
       for (int b = 1; b <= R; ++b) H[b][q] = f.add(p[-b * SJ], p[b * SJ]);
     }
+    double Q[2][R + 1][R + 1];
 #pragma unroll
     for (int o = 0; o < 2; ++o) {
-      double Q[R + 1][R + 1];
 #pragma unroll
       for (int b = 0; b <= R; ++b) {
-        Q[0][b] = H[b][R + o];
+        Q[o][0][b] = H[b][R + o];
 #pragma unroll
-        for (int c = 1; c <= R; ++c) Q[c][b] = f.add(H[b][R + o - c], H[b][R + o + c]);
+        for (int c = 1; c <= R; ++c) Q[o][c][b] = f.add(H[b][R + o - c], H[b][R + o + c]);
       }
       if constexpr (KJ) {
 #pragma unroll
         for (int c = 1; c <= R; ++c)
 #pragma unroll
-          for (int b = 0; b < c; ++b) Q[c][b] = f.add(Q[c][b], Q[b][c]);
+          for (int b = 0; b < c; ++b) Q[o][c][b] = f.add(Q[o][c][b], Q[o][b][c]);
       }
+    }
+    // W of both rows, one coefficient load per class and i distance (loaded at each use: held
+    // across the stream the coefficients would not fit the registers)
 #pragma unroll
-      for (int a = 0; a <= R; ++a) {
-        double w = 0.0;
+    for (int a = 0; a <= R; ++a) {
+      double w[2];
 #pragma unroll
-        for (int c = 0; c <= R; ++c)
+      for (int c = 0; c <= R; ++c)
 #pragma unroll
-          for (int b = 0; b <= (KJ ? c : R); ++b)
-            w = (c == 0 && b == 0) ? f.mul(cf[0][0][a], Q[0][0]) : fma(cf[c][b][a], Q[c][b], w);
+        for (int b = 0; b <= (KJ ? c : R); ++b) {
+          const double cf = f64_coef(tp, sym_index(c, b, a, R));
+#pragma unroll
+          for (int o = 0; o < 2; ++o) w[o] = (c == 0 && b == 0) ? f.mul(cf, Q[o][0][0]) : fma(cf, Q[o][c][b], w[o]);
+        }
+#pragma unroll
+      for (int o = 0; o < 2; ++o) {
 #pragma unroll
         for (int m = 0; m + 1 < NW; ++m) W[o][a][m] = W[o][a][m + 1];
-        W[o][a][NW - 1] = w;
+        W[o][a][NW - 1] = w[o];
       }
     }
   };
@@ -550,27 +565,25 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
 #pragma unroll
     for (int ii = RP - R; ii < RP + R; ++ii) column(ii);
   }
-  // the lane's outputs stay in registers: with no shared-memory stores in the column loop the
-  // loads of later columns may issue under the arithmetic of earlier ones
-  double outv[2][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     column(RP + R + i);  // the window now ends at column i + R: output i is complete
+    __syncwarp();        // every lane is past column RP + i
 #pragma unroll
     for (int o = 0; o < 2; ++o) {
       double v = W[o][0][R];
 #pragma unroll
       for (int a = 1; a <= R; ++a) v = f.add(v, f.add(W[o][a][R - a], W[o][a][R + a]));
-      outv[o][i] = v;
+      col[o * SK + RP + i] = v;
     }
   }
-  // rows (k0, j) and (k0 + 1, j) of the output brick, 16 bytes per store (the eight lanes of a
-  // plane cover 512 contiguous bytes in four stores)
+  __syncwarp();
+  // 64 outputs per store: lane l writes elements 2l, 2l + 1 of rows 8q .. 8q + 7
 #pragma unroll
-  for (int o = 0; o < 2; ++o)
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-      st_pair(ob + ((k0 + o) * 8 + j) * 8 + 2 * c, make_double2(outv[o][2 * c], outv[o][2 * c + 1]));
+  for (int q = 0; q < 8; ++q) {
+    const int e = q * 64 + 2 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
+    st_pair(ob + e, ld_pair(rt + (k + R) * SK + (jj + R) * SJ + RP + i));
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -828,7 +841,7 @@ __device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, 
 // threads (lt) owns one (j, i) column, or, for the column-pair cubes, each of the BJ*BI/2
 // threads a pair of columns.
 // out_brick: the output field's brick (field base + centre brick x step).
-// cs: the native FP64 register-operand block (F64Ops) in shared memory.
+// cs: the native FP64 register-operand block (F64Ops) in shared memory (stars and cubes).
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC>
 __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, const Taps &tp, const double *cs) {
   typedef Sweep2Cfg<T, BK, BJ, BI, R, FAM, ACC> C;
@@ -944,7 +957,7 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
         store_stream(ob + k * BJ * BI, acc.result());
       }
     }
-  } else if constexpr (C::F64R && FAM == FAM_STAR) {
+  } else if constexpr (C::F64S && FAM == FAM_STAR) {
     // the per-point operations of the star below, taps outer over the column's points, on
     // register operands (F64Ops), every multiply-add with its value freshly loaded
     const F64Ops f = F64Ops::load(cs);
@@ -966,7 +979,7 @@ __device__ __forceinline__ void sweep2_brick(const T *rt, T *out_brick, int lt, 
     }
 #pragma unroll
     for (int k = 0; k < BK; ++k) store_stream(reinterpret_cast<double *>(ob) + k * BJ * BI, acc[k]);
-  } else if constexpr (C::F64R && FAM == FAM_CUBE) {
+  } else if constexpr (C::F64S && FAM == FAM_CUBE) {
     // the per-point operations of the cube below ((dj, di) outer, dk inner), taps outer over the
     // column's points, on register operands (F64Ops), every multiply-add with its value freshly
     // loaded
@@ -1313,12 +1326,13 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
     cp_async_commit();
   };
 
-  // native FP64: the register-operand block (F64Ops), read after the prologue's barrier
+  // native FP64 stars and cubes: the register-operand block (F64Ops), read after the prologue's
+  // barrier
   const double *cs = reinterpret_cast<const double *>(smem_raw + NB * C::PER_BRICK);
-  if constexpr (C::F64R) {
+  if constexpr (C::F64S) {
     double *csw = reinterpret_cast<double *>(smem_raw + NB * C::PER_BRICK);
     for (int e = threadIdx.x; e < F64Ops::NHEAD + C::NCOEF; e += C::NT)
-      csw[e] = e == 0 ? tp.one : e == 1 ? tp.mzero : tp.c[C::CBASE + e - F64Ops::NHEAD];
+      csw[e] = e == 0 ? tp.one : e == 1 ? tp.mzero : tp.c[e - F64Ops::NHEAD];
   }
 
   // prologue: adjacency of the first two groups, copies of the first
@@ -1369,8 +1383,8 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
         T *ob = out + (size_t)nbr[13] * ostep;
         T *tile = const_cast<T *>(rt);  // this warp's buffer until the next barrier
         if constexpr (C::ES == 8) {
-          if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, cs, W, cont);
-          else sym_cube_istream<C, R, false>(tile, ob, lt, cs, W, cont);
+          if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, tp, W, cont);
+          else sym_cube_istream<C, R, false>(tile, ob, lt, tp, W, cont);
         } else {
           constexpr bool CM = ACC == ACCM_COMP;
           if (tp.kj) sym_cube_istream4<C, T, R, true, CM>(tile, ob, lt, tp, S4, cont);

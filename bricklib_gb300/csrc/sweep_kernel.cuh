@@ -84,6 +84,7 @@ struct Taps {
   // 1.0 and -0.0, which the native FP64 kernels hold in registers (F64Ops); set by the host so
   // that the compiler cannot fold them back into plain additions and products
   double one, mzero;
+  double one_mz[2];  // {1.0, -0.0}, read at a runtime index (F64Ops)
 };
 
 __host__ __device__ constexpr int sweep_threads(int tpb) { return tpb < 128 ? 128 : tpb; }
