@@ -513,6 +513,14 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
   // register operands (F64Ops): the class coefficients coef(c, b, a), 1 and -0
   static_assert(C::F64R && C::SYMF, "native FP64 classes");
   const F64Ops f = F64Ops::load(tp);
+  // the class coefficients coef(c, b, a), held for the brick
+  double cf[R + 1][R + 1][R + 1];
+#pragma unroll
+  for (int c = 0; c <= R; ++c)
+#pragma unroll
+    for (int b = 0; b <= (KJ ? c : R); ++b)
+#pragma unroll
+      for (int a = 0; a <= R; ++a) cf[c][b][a] = f64_coef(tp, sym_index(c, b, a, R));
   double *col = rt + (k0 + R) * SK + (j + R) * SJ;  // tile row of brick-local (k0, j), column 0
   // W_a of tile column ii for both rows, pushed into the window (newest at NW - 1)
   auto column = [&](const int ii) {
@@ -540,19 +548,17 @@ __device__ __forceinline__ void sym_cube_istream(double *rt, double *ob, const i
           for (int b = 0; b < c; ++b) Q[o][c][b] = f.add(Q[o][c][b], Q[o][b][c]);
       }
     }
-    // W of both rows, one coefficient load per class and i distance (loaded at each use: held
-    // across the stream the coefficients would not fit the registers)
+    // W of both rows
 #pragma unroll
     for (int a = 0; a <= R; ++a) {
       double w[2];
 #pragma unroll
       for (int c = 0; c <= R; ++c)
 #pragma unroll
-        for (int b = 0; b <= (KJ ? c : R); ++b) {
-          const double cf = f64_coef(tp, sym_index(c, b, a, R));
+        for (int b = 0; b <= (KJ ? c : R); ++b)
 #pragma unroll
-          for (int o = 0; o < 2; ++o) w[o] = (c == 0 && b == 0) ? f.mul(cf, Q[o][0][0]) : fma(cf, Q[o][c][b], w[o]);
-        }
+          for (int o = 0; o < 2; ++o)
+            w[o] = (c == 0 && b == 0) ? f.mul(cf[0][0][a], Q[o][0][0]) : fma(cf[c][b][a], Q[o][c][b], w[o]);
 #pragma unroll
       for (int o = 0; o < 2; ++o) {
 #pragma unroll
