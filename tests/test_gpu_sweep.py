@@ -309,6 +309,27 @@ def test_tma_star_kernel_equals_pipelined(dtype, acc, name, monkeypatch):
         assert int(np.count_nonzero((written != 0xFF).any(axis=1))) == nout
 
 
+@pytest.mark.parametrize("name", ["star7", "star13", "star25"])
+def test_fp64_register_operand_stars_equal_the_plain_operations(name, monkeypatch):
+    """The native FP64 star kernels that run on register operands (the first product as
+    fma(c, x, -0), coefficients in registers, taps outer over a column: the TMA-fed kernel and
+    the pipelined one) give the bits of the one-shot kernel, which multiplies and adds with
+    the coefficients as constant operands, point by point in the same order."""
+    st = stencils.make(name, 29)
+    dom = GridDomain((64, 64, 128), dtype=BK_F64)
+    arr = stencils.uniform(37, int(np.prod(dom.adims))).reshape(dom.adims)
+    # interior runs of signed zeros and of values whose products underflow exercise the -0 addend
+    o = dom.org
+    arr[o[0] + 3, o[1] + 5:o[1] + 9, o[2]:o[2] + 40] = -0.0
+    arr[o[0] + 9, o[1] + 2:o[1] + 6, o[2] + 8:o[2] + 48] = 1e-310
+    dom.set_field(0, arr)
+    dom.upload()
+    plain = _sweep_with("BK_SWEEP_ONESHOT", monkeypatch, dom, st, BK_ACC_NATIVE, dom.dev_interior)
+    for env in (None, "BK_SWEEP_PIPELINED"):
+        got = _sweep_with(env, monkeypatch, dom, st, BK_ACC_NATIVE, dom.dev_interior)
+        np.testing.assert_array_equal(got.view(np.uint8), plain.view(np.uint8), err_msg=str(env))
+
+
 def _row_lists(dom, seed):
     """Brick lists for the row-run kernel: grid order (full runs), a shuffle (runs of one),
     grid-order pieces of 1..9 bricks in shuffled order (runs cut at every alignment),
