@@ -603,12 +603,14 @@ def batched_record(ndom: int, tune: bool, reps: int = 5) -> dict:
         res = BT.autotune(w, _abi.BK_F32, _abi.BK_ACC_NATIVE, steps=steps, use_cache=False)
         best = res["best"]
         lay, cap, conc = B.Layout(tuple(best["bdim"]), tuple(best["fold"])), best["grid_cap"], best["concurrent"]
+        stg = best.get("stages", 0)
         tune_rec = {"seconds": round(time.perf_counter() - t0, 1), "table": res["table"]}
     else:
-        lay, cap, conc = B.DEFAULT_LAYOUT, 0, 1
+        lay, cap, conc, stg = B.DEFAULT_LAYOUT, 0, 1, 0
     bt = BT.Batch(w, lay, _abi.BK_F32)
     call("bk_batch_set_grid", bt.h, cap)
     call("bk_batch_set_concurrent", bt.h, conc)
+    call("bk_batch_set_stages", bt.h, stg)
     t_batch = BT.time_batch(bt, steps, reps=reps)
     gst_batch = w.points * steps / t_batch / 1e9
     npart = sum(1 for ds in bt.doms if ds.partial)
@@ -656,7 +658,7 @@ def batched_record(ndom: int, tune: bool, reps: int = 5) -> dict:
     rec = {"metric": "GStencil/s", "unit": "GStencil/s", "domains": len(w.domains), "interior_points": w.points,
            "steps": steps,
            "batched_fp32": {"value": round(gst_batch, 2), "ms_per_10_steps": round(t_batch * 1e3, 3),
-                            "layout": {"bdim": lay.bdim, "fold": lay.fold, "grid_cap": cap,
+                            "layout": {"bdim": lay.bdim, "fold": lay.fold, "grid_cap": cap, "stages": stg,
                                        "chosen_by": "autotuner" if tune else "default 8^3 bricks"},
                             "segments": "parallel graph branches" if conc else "one after another",
                             "partial_brick_domains": npart,

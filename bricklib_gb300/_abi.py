@@ -130,6 +130,9 @@ SIGNATURES = {
     "bk_batch_set_grid": (C.c_int, [_vp, C.c_int]),
     "bk_batch_run": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp]),
     "bk_batch_set_concurrent": (C.c_int, [_vp, C.c_int]),
+    "bk_batch_set_stages": (C.c_int, [_vp, C.c_int]),
+    "bk_set_pipeline_depth": (C.c_int, [C.c_int]),
+    "bk_get_pipeline_depth": (C.c_int, []),
     "bk_batch_parity": (C.c_int, [_vp]),
     "bk_batch_is_arena": (C.c_int, [_vp]),
     "bk_batch_destroy": (C.c_int, [_vp]),

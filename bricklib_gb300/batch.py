@@ -249,12 +249,15 @@ def time_batch(b: Batch, steps: int, reps: int = 3, stream=None) -> float:
 
 
 def autotune(w: Workload, dtype: int = BK_F32, acc: int = BK_ACC_NATIVE, steps: int = 10,
-             candidates=CANDIDATES, grid_caps=(0,), concurrency=(1, 0), use_cache: bool = True) -> Dict:
+             candidates=CANDIDATES, grid_caps=(0,), concurrency=(1, 0), stages=(0, 2, 3),
+             use_cache: bool = True) -> Dict:
     """Time every (brick dims, fold) candidate -- domains whose edges are not whole bricks
     padded to whole bricks with the cell-level wrap fill -- with the stencil segments of a step
-    as parallel graph branches or one after another (and any CTA caps given, which bound the
-    batch-mode kernels of domains in storages of their own); return the best with the full
-    table.  Results are cached per (workload, dtype, acc, GPU)."""
+    as parallel graph branches or one after another, and, on the layouts whose stars run the
+    TMA-fed kernels (8^3 row-major bricks), each pipeline depth in `stages` (0: the kernels'
+    defaults); any CTA caps given bound the batch-mode kernels of domains in storages of their
+    own.  Return the best with the full table.  Results are cached per (workload, dtype, acc,
+    GPU)."""
     import torch
     key = f"{w.signature()}:{dtype}:{acc}:{torch.cuda.get_device_name()}"
     cache = {}
@@ -273,13 +276,17 @@ def autotune(w: Workload, dtype: int = BK_F32, acc: int = BK_ACC_NATIVE, steps: 
             continue
         b = Batch(w, lay, dtype, acc)
         npart = sum(1 for ds in b.doms if ds.partial)
+        tma = tuple(bdim) == (8, 8, 8) and lay.row_major()
         for conc in concurrency:
             call("bk_batch_set_concurrent", b.h, conc)
-            for cap in grid_caps:
-                call("bk_batch_set_grid", b.h, cap)
-                t = time_batch(b, steps)
-                table.append({"bdim": bdim, "fold": fold, "concurrent": conc, "grid_cap": cap,
-                              "partial_domains": npart, "s_per_run": t, "gstencil_s": w.points * steps / t / 1e9})
+            for stg in (stages if tma else (0,)):
+                call("bk_batch_set_stages", b.h, stg)
+                for cap in grid_caps:
+                    call("bk_batch_set_grid", b.h, cap)
+                    t = time_batch(b, steps)
+                    table.append({"bdim": bdim, "fold": fold, "concurrent": conc, "stages": stg, "grid_cap": cap,
+                                  "partial_domains": npart, "s_per_run": t,
+                                  "gstencil_s": w.points * steps / t / 1e9})
         b.close()
         del b
     best = max((r for r in table if "gstencil_s" in r), key=lambda r: r["gstencil_s"])

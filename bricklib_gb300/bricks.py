@@ -196,6 +196,11 @@ class Layout:
         lane = ((k % fk) * fj + j % fj) * fi + i % fi
         return (vec * (fk * fj * fi) + lane).reshape(-1)
 
+    def row_major(self) -> bool:
+        """Whether every element sits at its row-major (k, j, i) offset (the layouts the
+        pipelined and TMA-fed kernels take)."""
+        return bool(np.array_equal(self.offsets(), np.arange(self.size)))
+
 
 DEFAULT_LAYOUT = Layout()
 

@@ -17,6 +17,7 @@
 
 #include "batch_common.cuh"
 #include "sweep2_kernel.cuh"
+#include "sweep3_kernel.cuh"
 
 namespace bk {
 
@@ -296,6 +297,7 @@ struct bk_batch {
   std::vector<std::pair<unsigned, unsigned>> seg;  // per stencil: (first work item, count)
   int parity = 0;
   int grid_cap = 0;
+  int stages = 0;  // pipeline depth of the TMA-fed star sweeps (0: the kernels' defaults)
   bool aligned = true;  // every field base and step 16-byte aligned: the pipelined kernel applies
   int *err = nullptr;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, fill, parity) -> graph
@@ -415,7 +417,12 @@ static int batch_sweep_segment(bk_batch *b, size_t q, cudaStream_t s) {
   if (!count) return BK_OK;
   if (b->arena) {
     const bk_field &fin = b->field[b->parity], &fout = b->field[b->parity ^ 1];
-    return bk_sweep(b->d_gadj, b->total, &fin, &fout, b->d_gwork + first, count, &b->csts[q], &b->lay, b->acc_mode, s);
+    const int prev = pipeline_depth_override();
+    set_pipeline_depth_override(b->stages);
+    const int st = bk_sweep(b->d_gadj, b->total, &fin, &fout, b->d_gwork + first, count, &b->csts[q], &b->lay,
+                            b->acc_mode, s);
+    set_pipeline_depth_override(prev);
+    return st;
   }
   return batch_launch_sweep(b->sts[q], b->dtype, b->d_doms, b->ndom, b->d_work + first, count, b->parity, b->L,
                             b->err, b->grid_cap, b->aligned, s);
@@ -743,6 +750,15 @@ int bk_batch_run(bk_batch *b, int steps, int fill_every, int use_graph, void *st
   }
   BK_CUDA(cudaGraphLaunch(it->second, user));
   if (steps % 2) b->parity ^= 1;
+  return BK_OK;
+}
+
+int bk_batch_set_stages(bk_batch *b, int stages) {
+  if (!b || (stages != 0 && (stages < 2 || stages > TMA_MAX_STAGES)))
+    return fail(BK_ERR_ARG, "bk_batch_set_stages: stages must be 0 or 2..4");
+  b->stages = stages;
+  for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
+  b->graphs.clear();
   return BK_OK;
 }
 

@@ -523,8 +523,11 @@ bool star_tma_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r,
 // copies brick by brick).
 bool row_group_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r, int nb, int slot_box,
                     TmaMaps *maps);
-// Pipeline depth: BK_TMA_STAGES (2..4) when set, else `dflt`.
+// Pipeline depth: the host thread's bk_set_pipeline_depth value when set, else BK_TMA_STAGES
+// (2..4) when set, else `dflt`.
 int tma_stages(int dflt);
+int pipeline_depth_override();
+void set_pipeline_depth_override(int stages);
 
 template <typename T, int BK, int BJ, int BI, int R, int ACC, bool NI>
 int launch_star_tma(const SweepArgs &a, const Taps &tp, int dtype, cudaStream_t s, int grid_cap = 0) {

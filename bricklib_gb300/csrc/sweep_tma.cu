@@ -87,7 +87,14 @@ bool row_group_maps(const SweepArgs &a, int dtype, int bk, int bj, int bi, int r
   return true;
 }
 
+// Pipeline depth of the TMA-fed star kernels on this host thread (bk_set_pipeline_depth; 0:
+// each kernel's default).
+static thread_local int g_stages = 0;
+int pipeline_depth_override() { return g_stages; }
+void set_pipeline_depth_override(int stages) { g_stages = stages; }
+
 int tma_stages(int dflt) {
+  if (g_stages >= 2 && g_stages <= TMA_MAX_STAGES) return g_stages;
   const char *e = getenv("BK_TMA_STAGES");
   if (!e) return dflt;
   const int v = atoi(e);
@@ -158,3 +165,14 @@ bool tma_eligible(const SweepPlan &p, const bk_field *in) {
 }
 
 }  // namespace bk
+
+using namespace bk;
+
+extern "C" int bk_set_pipeline_depth(int stages) {
+  if (stages != 0 && (stages < 2 || stages > TMA_MAX_STAGES))
+    return fail(BK_ERR_ARG, "bk_set_pipeline_depth: stages must be 0 (the kernels' defaults) or 2..4");
+  set_pipeline_depth_override(stages);
+  return BK_OK;
+}
+
+extern "C" int bk_get_pipeline_depth(void) { return pipeline_depth_override(); }

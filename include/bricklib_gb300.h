@@ -392,6 +392,15 @@ int bk_batch_set_grid(bk_batch *batch, int max_ctas);
  * then one launch per stencil sweeps that stencil's segment of the work list.  With use_graph the sequence is captured once per
  * (steps, fill_every, parity) into a CUDA graph kept by the batch and replayed on later calls. */
 int bk_batch_run(bk_batch *batch, int steps, int fill_every, int use_graph, void *stream);
+/* Pipeline depth (2..4 stages of staged bricks) of the TMA-fed star sweeps launched from the
+ * calling host thread; 0 restores each kernel's own default (3 for 4-byte radius-1 stars, else
+ * 2).  Fewer stages leave room for more resident CTAs.  Returns BK_ERR_ARG for other values. */
+int bk_set_pipeline_depth(int stages);
+/* The calling thread's setting (0: the kernels' defaults). */
+int bk_get_pipeline_depth(void);
+/* Pipeline depth of the batch's TMA-fed star sweeps (0: the kernels' defaults; see
+ * bk_set_pipeline_depth), the autotuner's launch-shape knob.  Drops the batch's captured graphs. */
+int bk_batch_set_stages(bk_batch *batch, int stages);
 /* on (default): the stencil segments of a step run as parallel branches (one stream each,
  * joined before the next step), so one segment's last wave overlaps the others' work; 0: one
  * after another on the caller's stream.  Drops the batch's captured graphs. */

@@ -2,7 +2,9 @@
 import numpy as np
 import pytest
 
-from bricklib_gb300 import batch as BT, bricks as B, stencils
+from bricklib_gb300 import _abi, batch as BT, bricks as B, stencils
+from bricklib_gb300._abi import call
+from bricklib_gb300.domain import GridDomain
 from bricklib_gb300._abi import BK_ACC_COMPENSATED, BK_ACC_NATIVE, BK_F32, BK_F64
 from oracle import oracle
 
@@ -130,6 +132,38 @@ def test_batch_graph_and_plain_bitwise_equal_and_layouts_agree():
             # only 8x8x8 bricks have the pair-sum path of mirror-symmetric cubes
             for x, y in zip(base, arrs):
                 assert np.abs(x - y).max() <= 1e-6 * np.abs(y).max()
+
+
+def test_pipeline_depth_leaves_the_bits_unchanged():
+    """The batch's pipeline-depth knob (the TMA-fed star kernels' stage count, one of the
+    autotuner's launch-shape settings) changes no result: every depth gives the bits of the
+    kernels' defaults, and so does the library-wide setting on a plain sweep."""
+    w = small_workload(nd=6, multiple=16, hi=64)
+    res = {}
+    for stg in (0, 2, 3, 4):
+        b = BT.Batch(w, B.Layout(), BK_F32)
+        call("bk_batch_set_stages", b.h, stg)
+        b.run(4, use_graph=True)
+        B.synchronize()
+        res[stg] = fields(b, b.parity)
+        b.close()
+    for stg in (2, 3, 4):
+        for x, y in zip(res[0], res[stg]):
+            np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8), err_msg=f"stages {stg}")
+    assert _abi.lib().bk_get_pipeline_depth() == 0  # the batch restored the caller's setting
+    dom = GridDomain(64, dtype=BK_F32)
+    dom.set_field(0, stencils.uniform(5, int(np.prod(dom.adims))).reshape(dom.adims))
+    dom.upload()
+    st = stencils.make("star13", 3)
+    outs = []
+    for stg in (0, 4):
+        call("bk_set_pipeline_depth", stg)
+        B.brickSweep(dom.brick(0), dom.brick(1), dom.dev_interior, st)
+        B.synchronize()
+        dom.download()
+        outs.append(dom.get_field(1))
+    call("bk_set_pipeline_depth", 0)
+    np.testing.assert_array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
 
 
 def test_domain_alone_equals_domain_in_the_mix():

@@ -152,6 +152,18 @@ def test_stencil_errors_are_reported_not_raised_in_c():
     assert e.value.status == _abi.BK_ERR_UNSUPPORTED
 
 
+def test_pipeline_depth_setting_is_checked():
+    """bk_set_pipeline_depth takes 0 (the kernels' defaults) or 2..4 stages and keeps the value
+    per host thread; anything else is BK_ERR_ARG and leaves the setting alone."""
+    lib = _abi.lib()
+    assert lib.bk_get_pipeline_depth() == 0
+    for bad in (1, 5, -2):
+        assert lib.bk_set_pipeline_depth(bad) == _abi.BK_ERR_ARG
+    assert lib.bk_get_pipeline_depth() == 0
+    assert lib.bk_set_pipeline_depth(3) == 0 and lib.bk_get_pipeline_depth() == 3
+    assert lib.bk_set_pipeline_depth(0) == 0 and lib.bk_get_pipeline_depth() == 0
+
+
 def test_periodic_plan_abi_matches_oracle():
     dom = GridDomain(16, device=False)
     plan = B.GhostPlan.__new__(B.GhostPlan)
