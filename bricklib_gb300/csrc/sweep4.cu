@@ -135,7 +135,12 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     const unsigned *nb = nbr[slot];
     if (nb[40] != NONE) {
       const unsigned base = (unsigned)__cvta_generic_to_shared(&tile[buf][0]);
-      for (int e = t; e < NENT; e += blockDim.x) {
+      // entries t, t + 256, ... of the table (256 threads: a compile-time count per thread)
+      constexpr int NPT = (NENT + 255) / 256;
+#pragma unroll
+      for (int m = 0; m < NPT; ++m) {
+        const int e = t + 256 * m;
+        if (e >= NENT) break;
         const unsigned w = plan[e];
         if (!w) continue;
         const T *src = in + (size_t)nb[w & 127u] * in_step;
@@ -171,6 +176,16 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
   const int oi = t % B, oj = (t / B) % B, ok = (t / (B * B)) % B, ol = t / (B * B * B);
   const int ctile = (((ol + R) * E + (ok + R)) * E + (oj + R)) * EI + (oi + RP);
   const int oofs = t < B * B * B * B ? L.offset(ol, ok, oj, oi) : 0;
+  // the tap list of a star of this radius fits MT entries: offsets held in registers for the
+  // whole kernel (the loop over a runtime count read them from the parameters per tap)
+  constexpr int MT = 8 * R + 1;
+  int toffr[MT];
+#pragma unroll
+  for (int q = 0; q < MT; ++q) toffr[q] = q < tp.n ? tp.toff[q] : 0;
+  auto coefq = [&](int q) -> AT {
+    if constexpr (sizeof(AT) == 8) return tp.c[q];
+    else return tp.cf[q];
+  };
   int jb = 0;
   for (unsigned long long n = n0; n < nlist; n += gs, ++jb) {
     const int cur = jb % 3, nxt = (jb + 1) % 3, far = (jb + 2) % 3, buf = jb & 1;
@@ -187,12 +202,16 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     if (ob != NONE && t < B * B * B * B) {
       const T *c = tile[buf] + ctile;
       AT v;
-      if constexpr (sizeof(AT) == 8) {
-        v = tp.c[0] * c[tp.toff[0]];
-        for (int q = 1; q < tp.n; ++q) v = fma(tp.c[q], c[tp.toff[q]], v);
+      if (tp.n <= MT) {
+        // up to MT taps (a radius-R star): unrolled, the offsets and coefficients from
+        // registers, the taps past n predicated off
+        v = coefq(0) * c[toffr[0]];
+#pragma unroll
+        for (int q = 1; q < MT; ++q)
+          if (q < tp.n) v = fma(coefq(q), c[toffr[q]], v);
       } else {
-        v = tp.cf[0] * c[tp.toff[0]];
-        for (int q = 1; q < tp.n; ++q) v = fmaf(tp.cf[q], c[tp.toff[q]], v);
+        v = coefq(0) * c[tp.toff[0]];
+        for (int q = 1; q < tp.n; ++q) v = fma(coefq(q), c[tp.toff[q]], v);
       }
       Elem<T>::store(out + (size_t)ob * out_step + oofs, v);
     }
