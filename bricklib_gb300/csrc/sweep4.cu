@@ -70,16 +70,20 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
   constexpr int B = 4, E = G::E, EI = G::EI, VE = G::VE, RP = G::RP, NBLK = G::NBLK, NENT = G::NENT, TILE = G::TILE;
   static_assert(TILE < (1 << 14), "tile offsets take 14 bits");
   constexpr unsigned NONE = 0xFFFFFFFFu;
-  // dynamic shared memory: tile[2][TILE], then the copy table: per (row, block) entry a word
-  // slot (7 bits) | tile offset (14) << 7 | element mask (VE bits) << 21 | kind << 30
-  // (0 nothing, 1 one 16-byte copy, 2 one copy per element of the mask) and a word of the
-  // elements' in-brick offsets (8 bits each)
+  // dynamic shared memory: tile[2][TILE], then the copy table (room for every (row, block);
+  // filled with the blocks that have elements to copy, nent of them, in any order): per entry
+  // a word slot (7 bits) | tile offset (14) << 7 | element mask (VE bits) << 21 | kind << 30
+  // (1 one 16-byte copy, 2 one copy per element of the mask) and a word of the elements'
+  // in-brick offsets (8 bits each)
   extern __shared__ __align__(16) unsigned char smem4[];
   T(*tile)[TILE] = reinterpret_cast<T(*)[TILE]>(smem4);
   unsigned *plan = reinterpret_cast<unsigned *>(smem4 + 2 * TILE * sizeof(T));
   unsigned *srcw = plan + NENT;
   __shared__ unsigned nbr[3][81];
+  __shared__ unsigned nent;  // entries of the compacted table
   const int t = threadIdx.x;
+  if (t == 0) nent = 0;
+  __syncthreads();
   for (int e = t; e < NENT; e += blockDim.x) {
     const int row = e / NBLK, blk = e - row * NBLK;
     const int l = row / (E * E) - R, k = (row / E) % E - R, j = row % E - R;  // in-brick, may lie outside
@@ -105,9 +109,12 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
       const unsigned slot = (unsigned)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
       const bool v16 = vec && consecutive && mask == (1u << VE) - 1u && s0 % VE == 0;
       w = slot | ((unsigned)(row * EI + blk * VE) << 7) | (mask << 21) | ((v16 ? 1u : 2u) << 30);
+      // only blocks with elements to copy enter the table (a star reads its centre and faces:
+      // 288 of 648 entries for FP32 radius 1), in any order
+      const unsigned at = atomicAdd(&nent, 1u);
+      plan[at] = w;
+      srcw[at] = sw;
     }
-    plan[e] = w;
-    srcw[e] = sw;
   }
   const unsigned long long gs = gridDim.x;
   // Staging of list entry n's adjacency row (thread t < 81 holds slot t): the list entry is
@@ -137,12 +144,12 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
       const unsigned base = (unsigned)__cvta_generic_to_shared(&tile[buf][0]);
       // entries t, t + 256, ... of the table (256 threads: a compile-time count per thread)
       constexpr int NPT = (NENT + 255) / 256;
+      const int ne = (int)nent;
 #pragma unroll
       for (int m = 0; m < NPT; ++m) {
         const int e = t + 256 * m;
-        if (e >= NENT) break;
+        if (e >= ne) break;
         const unsigned w = plan[e];
-        if (!w) continue;
         const T *src = in + (size_t)nb[w & 127u] * in_step;
         const unsigned dst = base + ((w >> 7) & 0x3FFFu) * (unsigned)sizeof(T);
         const unsigned sw = srcw[e];
