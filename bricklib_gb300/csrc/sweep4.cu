@@ -1,5 +1,5 @@
 // Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
-// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 256 threads: the
+// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 128 threads: the
 // part of a brick's neighbourhood the stencil reads (centre and faces for a star, the whole
 // radius-R box otherwise) is gathered into shared memory by asynchronous copies while the
 // previous brick is computed, one output per thread.  The copies follow a table the CTA builds
@@ -28,6 +28,7 @@ struct Taps4 {
   int toff[BK_MAX_TAPS4];  // offsets in the E x E x E x EI tile (Tile4)
   double c[BK_MAX_TAPS4];
   float cf[BK_MAX_TAPS4];
+  double mzero;  // -0.0: the addend that makes a product a multiply-add (FP64 register operands)
 };
 
 // Element copy global -> shared through the asynchronous copy path (4, 8 or 16 bytes).
@@ -59,8 +60,10 @@ struct Tile4 {
 // adjacency slots, so no slot is rewritten while read).  Two block barriers per brick.
 // star: every tap has at most one non-zero offset (only centre and face elements are read);
 // vec: the input field's bricks start 16-byte aligned (16-byte copies allowed).
+constexpr int NT4 = 128;  // threads per CTA, each computing two of a brick's 256 points
+
 template <typename T, typename AT, int R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(NT4)
 sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__restrict__ in, unsigned long long in_step,
               long long in_chunks, T *__restrict__ out, unsigned long long out_step, long long out_chunks,
               const unsigned *__restrict__ blist, unsigned nlist, const Layout4 L, const Taps4 tp, int star, int vec,
@@ -81,8 +84,13 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
   unsigned *srcw = plan + NENT;
   __shared__ unsigned nbr[3][81];
   __shared__ unsigned nent;  // entries of the compacted table
+  // FP64: the coefficients of a star of this radius and -0.0, read into per-thread registers
+  // (on GB300 a DFMA with a constant-bank coefficient, and a DMUL, issue a fifth slower)
+  constexpr int MT = 8 * R + 1;
+  __shared__ double cs4[MT + 1];
   const int t = threadIdx.x;
   if (t == 0) nent = 0;
+  if (t <= MT) cs4[t] = t == MT ? tp.mzero : t < tp.n ? tp.c[t] : 0.0;
   __syncthreads();
   for (int e = t; e < NENT; e += blockDim.x) {
     const int row = e / NBLK, blk = e - row * NBLK;
@@ -142,12 +150,12 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     const unsigned *nb = nbr[slot];
     if (nb[40] != NONE) {
       const unsigned base = (unsigned)__cvta_generic_to_shared(&tile[buf][0]);
-      // entries t, t + 256, ... of the table (256 threads: a compile-time count per thread)
-      constexpr int NPT = (NENT + 255) / 256;
+      // entries t, t + NT4, ... of the table (a compile-time count per thread)
+      constexpr int NPT = (NENT + NT4 - 1) / NT4;
       const int ne = (int)nent;
 #pragma unroll
       for (int m = 0; m < NPT; ++m) {
-        const int e = t + 256 * m;
+        const int e = t + NT4 * m;
         if (e >= ne) break;
         const unsigned w = plan[e];
         const T *src = in + (size_t)nb[w & 127u] * in_step;
@@ -178,20 +186,35 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
   unsigned bb = load_b(n0 + 3 * gs);  // list entry n + 3 gs
   __syncthreads();  // tables and the first two adjacency slots
   issue(0, 0);
-  // this thread's output element: its tile position and its in-brick offset (the layout's
-  // divisions by the fold, once per kernel instead of once per brick)
-  const int oi = t % B, oj = (t / B) % B, ok = (t / (B * B)) % B, ol = t / (B * B * B);
-  const int ctile = (((ol + R) * E + (ok + R)) * E + (oj + R)) * EI + (oi + RP);
-  const int oofs = t < B * B * B * B ? L.offset(ol, ok, oj, oi) : 0;
+  // this thread's output elements t and t + NT4: their tile positions and in-brick offsets (the
+  // layout's divisions by the fold, once per kernel instead of once per brick)
+  static_assert(2 * NT4 == B * B * B * B, "two points per thread");
+  int ctile[2], oofs[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int pt = t + NT4 * h;
+    const int oi = pt % B, oj = (pt / B) % B, ok = (pt / (B * B)) % B, ol = pt / (B * B * B);
+    ctile[h] = (((ol + R) * E + (ok + R)) * E + (oj + R)) * EI + (oi + RP);
+    oofs[h] = L.offset(ol, ok, oj, oi);
+  }
   // the tap list of a star of this radius fits MT entries: offsets held in registers for the
   // whole kernel (the loop over a runtime count read them from the parameters per tap)
-  constexpr int MT = 8 * R + 1;
   int toffr[MT];
 #pragma unroll
   for (int q = 0; q < MT; ++q) toffr[q] = q < tp.n ? tp.toff[q] : 0;
+  constexpr bool F64 = sizeof(AT) == 8;
+  AT cr[MT];
+#pragma unroll
+  for (int q = 0; q < MT; ++q) cr[q] = F64 ? (AT)cs4[q] : (AT)0;
+  const AT mz = F64 ? (AT)cs4[MT] : (AT)0;
   auto coefq = [&](int q) -> AT {
     if constexpr (sizeof(AT) == 8) return tp.c[q];
     else return tp.cf[q];
+  };
+  // the product of the first tap: FP64 as a multiply-add onto -0 (the same bits)
+  auto first = [&](AT k, AT x) -> AT {
+    if constexpr (F64) return fma(k, x, mz);
+    else return k * x;
   };
   int jb = 0;
   for (unsigned long long n = n0; n < nlist; n += gs, ++jb) {
@@ -206,21 +229,33 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     cp_async_wait4<1>();  // this thread's copies for brick n have landed
     __syncthreads();      // ... and everybody else's
     const unsigned ob = nbr[cur][40];
-    if (ob != NONE && t < B * B * B * B) {
-      const T *c = tile[buf] + ctile;
-      AT v;
+    if (ob != NONE) {
+      const T *c0 = tile[buf] + ctile[0], *c1 = tile[buf] + ctile[1];
+      AT v0, v1;
       if (tp.n <= MT) {
         // up to MT taps (a radius-R star): unrolled, the offsets and coefficients from
-        // registers, the taps past n predicated off
-        v = coefq(0) * c[toffr[0]];
+        // registers, the taps past n predicated off; the thread's two points side by side
+        const AT k0 = F64 ? cr[0] : coefq(0);
+        v0 = first(k0, c0[toffr[0]]);
+        v1 = first(k0, c1[toffr[0]]);
 #pragma unroll
         for (int q = 1; q < MT; ++q)
-          if (q < tp.n) v = fma(coefq(q), c[toffr[q]], v);
+          if (q < tp.n) {
+            const AT kq = F64 ? cr[q] : coefq(q);
+            v0 = fma(kq, c0[toffr[q]], v0);
+            v1 = fma(kq, c1[toffr[q]], v1);
+          }
       } else {
-        v = coefq(0) * c[tp.toff[0]];
-        for (int q = 1; q < tp.n; ++q) v = fma(coefq(q), c[tp.toff[q]], v);
+        v0 = coefq(0) * c0[tp.toff[0]];
+        v1 = coefq(0) * c1[tp.toff[0]];
+        for (int q = 1; q < tp.n; ++q) {
+          v0 = fma(coefq(q), c0[tp.toff[q]], v0);
+          v1 = fma(coefq(q), c1[tp.toff[q]], v1);
+        }
       }
-      Elem<T>::store(out + (size_t)ob * out_step + oofs, v);
+      T *ob0 = out + (size_t)ob * out_step;
+      Elem<T>::store(ob0 + oofs[0], v0);
+      Elem<T>::store(ob0 + oofs[1], v1);
     }
   }
   cp_async_wait4<0>();  // no copy may outlive the kernel
@@ -243,12 +278,12 @@ static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, co
   cudaError_t e0 = cudaGetDevice(&dev);
   if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e0 == cudaSuccess && smem > 48 * 1024) e0 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e0 == cudaSuccess) e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+  if (e0 == cudaSuccess) e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT4, smem);
   if (e0 != cudaSuccess) return cuda_fail(e0, "sweep4 launch setup");
   long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
   if (grid > nlist) grid = nlist;
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, 256, smem, s>>>(
+  kern<<<(unsigned)grid, NT4, smem, s>>>(
       adj, nbricks, reinterpret_cast<const T *>(in->dat) + in->offset, in->step, in->chunks,
       reinterpret_cast<T *>(out->dat) + out->offset, out->step, out->chunks, blist, nlist, L, tp, star, vec, err);
   cudaError_t e = cudaGetLastError();
@@ -291,6 +326,7 @@ int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const b
   const int R = r <= 1 ? 1 : 2;
   Taps4 tp;
   tp.n = st->npoints;
+  tp.mzero = -0.0;
   int star = 1;
   for (int t = 0; t < tp.n; ++t) {
     const int *o = st->offsets[t];
