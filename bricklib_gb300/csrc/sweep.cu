@@ -80,8 +80,6 @@ static int analyze(const bk_stencil *st, const Layout &L, SweepPlan *plan, Taps 
   tp->n = n;
   tp->pre = st->pre_op;
   tp->post = st->post_op;
-  tp->one = 1.0;
-  tp->mzero = -0.0;
   tp->one_mz[0] = 1.0;
   tp->one_mz[1] = -0.0;
   static thread_local int offs[BK_MAX_TAPS][3];

@@ -46,7 +46,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // of the plain operations: 1 * a is exact and -0 is the identity of every sum (signed zeros
 // included), so each form rounds once, as the plain operation does.  The operands come either
 // from a shared-memory block (F64Ops::NHEAD doubles, then the coefficients, filled from
-// Taps::one / mzero / c) or straight from the kernel parameters at an index that carries a
+// Taps::one_mz and c) or straight from the kernel parameters at an index that carries a
 // per-thread zero the compiler cannot see through: the loads then land in per-thread registers
 // (a parameter read at a uniform index measured as slow as a constant-bank operand: cube27
 // 19.0 against 22.4 GStencil/s), are neither merged nor hoisted, and cost no shared memory.
@@ -1338,7 +1338,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   if constexpr (C::F64S) {
     double *csw = reinterpret_cast<double *>(smem_raw + NB * C::PER_BRICK);
     for (int e = threadIdx.x; e < F64Ops::NHEAD + C::NCOEF; e += C::NT)
-      csw[e] = e == 0 ? tp.one : e == 1 ? tp.mzero : tp.c[e - F64Ops::NHEAD];
+      csw[e] = e < F64Ops::NHEAD ? tp.one_mz[e] : tp.c[e - F64Ops::NHEAD];
   }
 
   // prologue: adjacency of the first two groups, copies of the first

@@ -341,7 +341,7 @@ sweep_star_tma_kernel(const __grid_constant__ TmaMaps maps, const SweepArgs a, c
   static_assert(C::NT >= F64Ops::NHEAD + C::NTAP, "one thread per entry");
   double *coef_s = reinterpret_cast<double *>(sm + S * NB * C::BRICK + C::O_COEF);
   if (threadIdx.x < F64Ops::NHEAD + C::NTAP)
-    coef_s[threadIdx.x] = threadIdx.x == 0 ? tp.one : threadIdx.x == 1 ? tp.mzero : tp.c[threadIdx.x - F64Ops::NHEAD];
+    coef_s[threadIdx.x] = threadIdx.x < F64Ops::NHEAD ? tp.one_mz[threadIdx.x] : tp.c[threadIdx.x - F64Ops::NHEAD];
   __syncthreads();
 
   const long long ngroups = ((long long)a.nlist + NB - 1) / NB;

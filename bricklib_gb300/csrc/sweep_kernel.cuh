@@ -81,10 +81,9 @@ struct Taps {
   int kj;                  // mirror-symmetric cube also symmetric under the k <-> j swap
   // mirror-symmetric cubes: (cf, cf) of class (|dk|, |dj|, |di|) at ((|dk| (R+1) + |dj|) (R+1) + |di|)
   float2 sp[27];
-  // 1.0 and -0.0, which the native FP64 kernels hold in registers (F64Ops); set by the host so
+  // {1.0, -0.0}, which the native FP64 kernels hold in registers (F64Ops); set by the host so
   // that the compiler cannot fold them back into plain additions and products
-  double one, mzero;
-  double one_mz[2];  // {1.0, -0.0}, read at a runtime index (F64Ops)
+  double one_mz[2];
 };
 
 __host__ __device__ constexpr int sweep_threads(int tpb) { return tpb < 128 ? 128 : tpb; }
