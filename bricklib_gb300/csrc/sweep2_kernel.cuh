@@ -127,6 +127,12 @@ __host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, in
 
 // bricks (warps) per CTA of the column-pair cube kernels: one, so that a CTA's barriers wait
 // for no other warp (GB300, FP32 cube125 at 512^3: 191 / 171 GStencil/s with one / two)
+// class-sum streams of 4- / 2-byte storage: about this many consecutive groups per chunk of a
+// CTA's walk
+#ifndef BK_CS_CHUNK
+#define BK_CS_CHUNK 16
+#endif
+
 #ifndef BK_PAIR_NB
 #define BK_PAIR_NB 1
 #endif
@@ -1197,7 +1203,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   const long long G = gridDim.x;
   long long CH = 1;
   if constexpr (CHUNKED) {
-    const long long rounds = (ngroups + G * 16 - 1) / (G * 16);
+    const long long rounds = (ngroups + G * BK_CS_CHUNK - 1) / (G * BK_CS_CHUNK);
     CH = (ngroups + G * rounds - 1) / (G * rounds);
     if (CH < 1) CH = 1;
   }
