@@ -708,9 +708,18 @@ def run_serving(args):
             st = serving.run_load(rate, args.njobs, fp64_acc=acc)
             st["fp64_arithmetic"] = acc_name
             res.append(st)
+    # the served FP32 form against the plain path on the same mixed-size jobs: all jobs FP32,
+    # offered faster than the server completes them (its throughput), and the same jobs run one
+    # by one through the plain drop-in path (FP64 storage)
+    fp32 = serving.run_load(20000.0, args.njobs, fp64_frac=0.0)
+    fp32["job_mix"] = "all FP32, otherwise as above"
+    plain = serving.plain_rate(args.njobs, fp64_frac=0.0, dtype=_abi.BK_F64)
     if rank == 0:
         print(json.dumps({"form": "serving", "metric": "p50/p99 latency (s), GStencil/s", "budget_bytes": 150e9,
-                          "jobs": SERVING_JOBS, "runs": res}), flush=True)
+                          "jobs": SERVING_JOBS, "runs": res, "served_fp32": fp32,
+                          "plain_fp64_same_jobs": plain,
+                          "served_fp32_vs_plain_fp64": round(fp32["gstencil_s"] / plain["gstencil_s"], 2)}),
+              flush=True)
 
 
 def forms_record(args) -> dict:

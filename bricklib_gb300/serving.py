@@ -83,7 +83,9 @@ class JobSpec:
 
 
 def make_jobs(njobs: int, seed: int = 11, lo: int = 16, hi: int = 192, max_steps: int = 200,
-              shapes: Sequence[str] = stencils.PLAIN_SHAPES) -> List[JobSpec]:
+              shapes: Sequence[str] = stencils.PLAIN_SHAPES, fp64_frac: float = 0.5) -> List[JobSpec]:
+    """Seeded jobs: edges log-uniform on [lo, hi] (multiples of 8), a shape, steps uniform on
+    [1, max_steps], FP64 storage with probability fp64_frac, else FP32."""
     u = stencils.uniform01(seed, njobs * 6)
     jobs = []
     for q in range(njobs):
@@ -91,7 +93,7 @@ def make_jobs(njobs: int, seed: int = 11, lo: int = 16, hi: int = 192, max_steps
              for a in range(3)]
         shape = shapes[int(u[6 * q + 3] * len(shapes)) % len(shapes)]
         steps = 1 + int(u[6 * q + 4] * max_steps) % max_steps
-        dtype = BK_F64 if u[6 * q + 5] < 0.5 else BK_F32
+        dtype = BK_F64 if u[6 * q + 5] < fp64_frac else BK_F32
         jobs.append(JobSpec(tuple(e), shape, steps, dtype, seed * 7919 + q))
     return jobs
 
@@ -119,9 +121,9 @@ def job_arrays(jobs: Sequence[JobSpec], pinned: bool = True):
 
 
 def run_load(rate: float, njobs: int, seed: int = 11, budget: float = 150e9, fp64_acc: int = BK_ACC_NATIVE,
-             max_active: int = 1024) -> dict:
+             max_active: int = 1024, fp64_frac: float = 0.5) -> dict:
     """Poisson arrivals at `rate` jobs/s of `njobs` jobs; returns the server statistics."""
-    jobs = make_jobs(njobs, seed)
+    jobs = make_jobs(njobs, seed, fp64_frac=fp64_frac)
     arena, ins, outs = job_arrays(jobs)
     sts = {s: B.to_c_stencil(stencils.make(s, 5)) for s in stencils.PLAIN_SHAPES}
     srv = Server(budget, max_active=max_active)
@@ -146,3 +148,31 @@ def run_load(rate: float, njobs: int, seed: int = 11, budget: float = 150e9, fp6
                "offered_point_steps": float(sum(j.points * j.steps for j in jobs))})
     del arena
     return st
+
+
+def plain_rate(njobs: int, seed: int = 11, fp64_frac: float = 0.5, dtype: int = BK_F64, stream=None) -> dict:
+    """The jobs of run_load(njobs, seed, fp64_frac=...) run one after another through the plain
+    drop-in path instead (each its own 8^3-brick domain with ghost bricks, a periodic ghost fill
+    before every step, `dtype` storage): device time of the steps (CUDA events; set-up and copies
+    excluded) and the aggregate GStencil/s, the comparator of the served rate."""
+    import torch
+    from . import batch as BT
+    jobs = make_jobs(njobs, seed, fp64_frac=fp64_frac)
+    s = torch.cuda.current_stream() if stream is None else stream
+    w_st = [stencils.make(x, 5) for x in stencils.PLAIN_SHAPES]
+    tot, work = 0.0, 0.0
+    for j in jobs:
+        ds = BT.DomainStorage(BT.DomainSpec(j.n, stencils.PLAIN_SHAPES.index(j.shape), j.seed), B.DEFAULT_LAYOUT, dtype)
+        BT.init_domain(ds, s.cuda_stream)
+        plan, lst = B.GhostPlan(ds.pairs), B.BrickList(ds.interior)
+        st = B.to_c_stencil(w_st[stencils.PLAIN_SHAPES.index(j.shape)])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        B.timeSteps(ds.field(0), ds.field(1), lst, st, j.steps, plan=plan, stream=s.cuda_stream)
+        e1.record(s)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1) * 1e-3
+        work += float(j.points * j.steps)
+        del ds
+    return {"jobs": njobs, "seconds": tot, "point_steps": work, "gstencil_s": work / tot / 1e9}
