@@ -44,12 +44,13 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // native FP64 kernels write a + b as fma(1, a, b) and c * x as fma(c, x, -0), with 1 and -0 in
 // registers, and read their coefficients from shared memory into registers.  The bits are those
 // of the plain operations: 1 * a is exact and -0 is the identity of every sum (signed zeros
-// included), so each form rounds once, as the plain operation does.  The operands come either
-// from a shared-memory block (F64Ops::NHEAD doubles, then the coefficients, filled from
-// Taps::one_mz and c) or straight from the kernel parameters at an index that carries a
-// per-thread zero the compiler cannot see through: the loads then land in per-thread registers
-// (a parameter read at a uniform index measured as slow as a constant-bank operand: cube27
-// 19.0 against 22.4 GStencil/s), are neither merged nor hoisted, and cost no shared memory.
+// included), so each form rounds once, as the plain operation does.  The operands come from a
+// shared-memory block (F64Ops::NHEAD doubles, then the coefficients, filled from Taps::one_mz
+// and c; stars and cubes), or, for the class-sum stream, whose tile leaves no room for the
+// block without losing a resident CTA per SM, straight from the kernel parameters at an index
+// carrying a zero the compiler cannot see through (so the loads are neither folded into
+// constant operands nor hoisted).  Measured: the stream runs the same from either source; the
+// 27-point cube ran 22.4 GStencil/s from the shared block and 19.0 from parameter loads.
 __device__ __forceinline__ int opaque_zero() {
   int z;
   asm volatile("mov.u32 %0, 0;\n" : "=r"(z));
