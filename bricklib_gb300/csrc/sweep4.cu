@@ -1,31 +1,34 @@
 // Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
 // tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 128 threads: the
 // part of a brick's neighbourhood the stencil reads (centre and faces for a star, the whole
-// radius-R box otherwise) is gathered into shared memory by asynchronous copies while the
-// previous brick is computed, one output per thread.  The copies follow a table the CTA builds
-// once from the layout: one entry per 16-byte block of a tile row, a single 16-byte copy where
-// the block's elements are consecutive in their brick, else one copy per element.  Out-of-range
-// list or adjacency entries are clamped / skipped and raise the device error flag, as in the
-// 3-D kernels.
+// radius-R box otherwise) is gathered into shared memory by asynchronous copies while earlier
+// bricks are computed (two bricks in flight for radius 1), two outputs per thread.  The copies
+// follow a table the CTA builds once from the layout: one entry per 16-byte block of a tile
+// row's centre and one per i-halo side, a single 16-byte copy where the block's elements are
+// consecutive in their brick, else one copy per element.  Out-of-range list or adjacency
+// entries are clamped / skipped and raise the device error flag, as in the 3-D kernels.
 #include "bk_common.cuh"
 
 namespace bk {
 
 struct Layout4 {
   int b[4], f[4];  // (l, k, j, i), outermost first
+  int lf[4];       // log2 of the folds: a fold divides the brick's 4, so it is 1, 2 or 4
   __host__ __device__ __forceinline__ int size() const { return b[0] * b[1] * b[2] * b[3]; }
-  // in-brick offset: folds right-aligned, vector index over the fold blocks, lane inside
+  // in-brick offset of (l, k, j, i), each in [0, 4): folds right-aligned, vector index over
+  // the fold blocks, lane inside (the reference's accessor formula, with shifts and masks)
   __host__ __device__ __forceinline__ int offset(int l, int k, int j, int i) const {
     const int vl = f[0] * f[1] * f[2] * f[3];
-    const int vec = (((l / f[0]) * (b[1] / f[1]) + k / f[1]) * (b[2] / f[2]) + j / f[2]) * (b[3] / f[3]) + i / f[3];
-    const int lane = (((l % f[0]) * f[1] + k % f[1]) * f[2] + j % f[2]) * f[3] + i % f[3];
+    const int vec = ((((l >> lf[0]) * (4 >> lf[1]) + (k >> lf[1])) * (4 >> lf[2]) + (j >> lf[2])) * (4 >> lf[3])) +
+                    (i >> lf[3]);
+    const int lane = (((l & (f[0] - 1)) * f[1] + (k & (f[1] - 1))) * f[2] + (j & (f[2] - 1))) * f[3] + (i & (f[3] - 1));
     return vec * vl + lane;
   }
 };
 
 struct Taps4 {
   int n;
-  int toff[BK_MAX_TAPS4];  // offsets in the E x E x E x EI tile (Tile4)
+  int toff[BK_MAX_TAPS4];  // tile offsets (Tile4::toff)
   double c[BK_MAX_TAPS4];
   float cf[BK_MAX_TAPS4];
   double mzero;  // -0.0: the addend that makes a product a multiply-add (FP64 register operands)
@@ -43,106 +46,139 @@ __device__ __forceinline__ void cp_async_commit4() { asm volatile("cp.async.comm
 template <int N>
 __device__ __forceinline__ void cp_async_wait4() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Tile of one brick's neighbourhood: E = 4 + 2R along l, k, j; along i the halo is rounded up
-// to whole 16-byte blocks (RP elements a side), EI = 4 + 2 RP, so that each block of a row lies
-// in one brick and the centre blocks start 16-byte aligned.
-template <typename T, int R>
+// Tile of one brick's neighbourhood: E = 4 + 2R rows along each of l, k, j.  A row holds its 4
+// centre elements from C0 (a whole number of 16-byte blocks, >= R) and R halo elements either
+// side; the rows of an (l, k) plane are P apart (P >= 4 + 2R, a whole number of blocks) and the
+// planes Q apart, so row (l, k, j) spans [(l E + k) Q + j P + C0 - R, ... + C0 + 4 + R): a row's
+// i-hi halo may share a 16-byte block with the unused front of the next row, and every centre
+// block starts 16-byte aligned.  For 4-byte storage Q = E P + 4: the two k planes a warp's
+// points span then fall on complementary shared-memory banks (E P alone is 0 or 16 mod 32).
+// A tap (dl, dk, dj, di) is the fixed tile offset (dl E + dk) Q + dj P + di from any point.
+// STARONLY: the table holds a star's centre and face elements only.
+template <typename T, int R, bool STARONLY>
 struct Tile4 {
-  static constexpr int ES = (int)sizeof(T), VE = 16 / ES, RP = (R + VE - 1) / VE * VE;
-  static constexpr int E = 4 + 2 * R, EI = 4 + 2 * RP, ROWS = E * E * E, NBLK = EI / VE;
-  static constexpr int NENT = ROWS * NBLK, TILE = ROWS * EI;
-  static constexpr size_t SMEM = 2 * (size_t)TILE * ES + (size_t)NENT * 8;
+  static constexpr int ES = (int)sizeof(T), VE = 16 / ES;
+  static constexpr int C0 = (R + VE - 1) / VE * VE, P = (4 + 2 * R + VE - 1) / VE * VE;
+  static constexpr int E = 4 + 2 * R, ROWS = E * E * E, NBC = 4 / VE, NSEG = NBC + 2;
+  static constexpr int Q = E * P + (ES == 4 ? 4 : 0);
+  static constexpr int TILE = (E * E - 1) * Q + (E - 1) * P + C0 + 4 + R;
+  // copy table words: one per tile element the stencil can read, at most
+  static constexpr int NTAB = STARONLY ? 256 + 512 * R : ROWS * (4 + 2 * R);
+  // tile buffers: S - 1 bricks in flight (FP64 sweeps are bound by the FP64 pipe and keep the
+  // resident CTAs instead)
+  static constexpr int S = (R == 1 && ES == 4) ? 3 : 2;
+  static constexpr int TILEA = (TILE + VE - 1) / VE * VE;  // buffer stride, whole 16-byte blocks
+  static constexpr size_t SMEM = S * (size_t)TILEA * ES + (size_t)NTAB * 4;
+  __host__ __device__ static constexpr int toff(int dl, int dk, int dj, int di) { return (dl * E + dk) * Q + dj * P + di; }
 };
 
-// Persistent CTAs walk the brick list with a stride of the grid, pipelined: while brick j is
-// computed from one tile buffer, brick j+1's neighbourhood is gathered into the other by
-// asynchronous copies, and brick j+2's list and adjacency entries are staged (three
-// adjacency slots, so no slot is rewritten while read).  Two block barriers per brick.
+// Persistent CTAs walk the brick list with a stride of the grid, pipelined over S tile buffers:
+// while brick j is computed, the neighbourhoods of bricks j+1 .. j+S-1 are being gathered by
+// asynchronous copies, brick j+S's list and adjacency entries are staged into shared memory
+// (S + 1 adjacency slots, so no slot is rewritten while read), brick j+S+1's and j+S+2's
+// adjacency entries and brick j+S+3's list entry are in flight in registers.  Only the
+// adjacency slots the tile reads are staged (9 of 81 for a star), by the CTA's last threads.
+// One block barrier per brick.
 // star: every tap has at most one non-zero offset (only centre and face elements are read);
+// canon: the taps are exactly the star of radius R, passed in the order centre, then along l,
+// k, j, i the distances -R..-1, 1..R (tile offsets known at compile time);
 // vec: the input field's bricks start 16-byte aligned (16-byte copies allowed).
 constexpr int NT4 = 128;  // threads per CTA, each computing two of a brick's 256 points
 
-template <typename T, typename AT, int R>
+template <typename T, typename AT, int R, bool CANON>
 __global__ void __launch_bounds__(NT4)
 sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__restrict__ in, unsigned long long in_step,
               long long in_chunks, T *__restrict__ out, unsigned long long out_step, long long out_chunks,
               const unsigned *__restrict__ blist, unsigned nlist, const Layout4 L, const Taps4 tp, int star, int vec,
               int *err) {
   static_assert(sizeof(T) == sizeof(AT) && (sizeof(T) == 4 || sizeof(T) == 8), "the tile holds the storage type");
-  typedef Tile4<T, R> G;
-  constexpr int B = 4, E = G::E, EI = G::EI, VE = G::VE, RP = G::RP, NBLK = G::NBLK, NENT = G::NENT, TILE = G::TILE;
-  static_assert(TILE < (1 << 14), "tile offsets take 14 bits");
+  typedef Tile4<T, R, CANON> G;
+  constexpr int B = 4, E = G::E, VE = G::VE, C0 = G::C0, NBC = G::NBC, NSEG = G::NSEG;
+  constexpr int NTAB = G::NTAB, TILEA = G::TILEA, S = G::S, NSLOT = S + 1;
+  static_assert(G::TILE < (1 << 14), "tile offsets take 14 bits");
   constexpr unsigned NONE = 0xFFFFFFFFu;
-  // dynamic shared memory: tile[2][TILE], then the copy table (room for every (row, block);
-  // filled with the blocks that have elements to copy, nent of them, in any order): per entry
-  // a word slot (7 bits) | tile offset (14) << 7 | element mask (VE bits) << 21 | kind << 30
-  // (1 one 16-byte copy, 2 one copy per element of the mask) and a word of the elements'
-  // in-brick offsets (8 bits each)
+  // dynamic shared memory: tile[S][TILEA], then the copy table, one word per copy: adjacency
+  // slot (7 bits) | tile offset (14) << 7 | in-brick offset of the (first) element (8) << 21.
+  // 16-byte copies fill it from the front (n16 of them), one-element copies from the back (nel).
   extern __shared__ __align__(16) unsigned char smem4[];
-  T(*tile)[TILE] = reinterpret_cast<T(*)[TILE]>(smem4);
-  unsigned *plan = reinterpret_cast<unsigned *>(smem4 + 2 * TILE * sizeof(T));
-  unsigned *srcw = plan + NENT;
-  __shared__ unsigned nbr[3][81];
-  __shared__ unsigned nent;  // entries of the compacted table
+  T(*tile)[TILEA] = reinterpret_cast<T(*)[TILEA]>(smem4);
+  unsigned *plan = reinterpret_cast<unsigned *>(smem4 + S * TILEA * sizeof(T));
+  __shared__ unsigned nbr[NSLOT][81];
+  __shared__ unsigned n16, nel, needm[3], nneed;
+  __shared__ unsigned char need[81];  // the adjacency slots the tile reads, the centre (40) first
   // FP64: the coefficients of a star of this radius and -0.0, read into per-thread registers
   // (on GB300 a DFMA with a constant-bank coefficient, and a DMUL, issue a fifth slower)
   constexpr int MT = 8 * R + 1;
   __shared__ double cs4[MT + 1];
   const int t = threadIdx.x;
-  if (t == 0) nent = 0;
+  if (t == 0) {
+    n16 = nel = 0;
+    needm[0] = needm[2] = 0;
+    needm[1] = 1u << (40 - 32);
+  }
   if (t <= MT) cs4[t] = t == MT ? tp.mzero : t < tp.n ? tp.c[t] : 0.0;
   __syncthreads();
-  for (int e = t; e < NENT; e += blockDim.x) {
-    const int row = e / NBLK, blk = e - row * NBLK;
+  for (int e = t; e < G::ROWS * NSEG; e += blockDim.x) {
+    const int row = e / NSEG, seg = e - row * NSEG;
     const int l = row / (E * E) - R, k = (row / E) % E - R, j = row % E - R;  // in-brick, may lie outside
     const int ql = l < 0 ? -1 : (l >= B ? 1 : 0), qk = k < 0 ? -1 : (k >= B ? 1 : 0);
     const int qj = j < 0 ? -1 : (j >= B ? 1 : 0);
-    const int i0 = blk * VE - RP;  // the block's first i
-    const int qi = i0 < 0 ? -1 : (i0 >= B ? 1 : 0);
+    // the segment: one 16-byte block of the row's centre, or the R halo elements on one side
+    const int qi = seg < NBC ? 0 : (seg == NBC ? -1 : 1);
+    const int i0 = seg < NBC ? seg * VE : (seg == NBC ? -R : B);
+    const int cnt = seg < NBC ? VE : R;
+    const int dst0 = (row / E) * G::Q + (row % E) * G::P + C0 + i0;
     const int outside = (ql != 0) + (qk != 0) + (qj != 0) + (qi != 0);
-    unsigned mask = 0, sw = 0;
+    if (star && outside > 1) continue;  // a star reads centre and face elements only
+    const unsigned slot = (unsigned)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
+    int so[VE];
     bool consecutive = true;
-    int s0 = -1;
+#pragma unroll
     for (int q = 0; q < VE; ++q) {
-      const int i = i0 + q;
-      if (i < -R || i >= B + R || (star && outside > 1)) continue;
-      const int so = L.offset(l - ql * B, k - qk * B, j - qj * B, i - qi * B);
-      if (q == 0) s0 = so;
-      if (so != s0 + q) consecutive = false;
-      mask |= 1u << q;
-      sw |= (unsigned)so << (8 * q);
+      so[q] = q < cnt ? L.offset(l - ql * B, k - qk * B, j - qj * B, i0 + q - qi * B) : 0;
+      if (q < cnt && so[q] != so[0] + q) consecutive = false;
     }
-    unsigned w = 0;
-    if (mask) {
-      const unsigned slot = (unsigned)(((ql + 1) * 3 + (qk + 1)) * 9 + (qj + 1) * 3 + (qi + 1));
-      const bool v16 = vec && consecutive && mask == (1u << VE) - 1u && s0 % VE == 0;
-      w = slot | ((unsigned)(row * EI + blk * VE) << 7) | (mask << 21) | ((v16 ? 1u : 2u) << 30);
-      // only blocks with elements to copy enter the table (a star reads its centre and faces:
-      // 288 of 648 entries for FP32 radius 1), in any order
-      const unsigned at = atomicAdd(&nent, 1u);
-      plan[at] = w;
-      srcw[at] = sw;
+    atomicOr(&needm[slot >> 5], 1u << (slot & 31u));
+    if (vec && consecutive && cnt == VE && so[0] % VE == 0 && dst0 % VE == 0) {
+      plan[atomicAdd(&n16, 1u)] = slot | ((unsigned)dst0 << 7) | ((unsigned)so[0] << 21);
+    } else {
+#pragma unroll
+      for (int q = 0; q < VE; ++q)
+        if (q < cnt) plan[NTAB - 1 - atomicAdd(&nel, 1u)] = slot | ((unsigned)(dst0 + q) << 7) | ((unsigned)so[q] << 21);
     }
   }
+  __syncthreads();
+  if (t == 0) {
+    unsigned c = 0;
+    need[c++] = 40;
+    for (int q = 0; q < 81; ++q)
+      if (q != 40 && ((needm[q >> 5] >> (q & 31)) & 1u)) need[c++] = (unsigned char)q;
+    nneed = c;
+  }
+  __syncthreads();
   const unsigned long long gs = gridDim.x;
-  // Staging of list entry n's adjacency row (thread t < 81 holds slot t): the list entry is
-  // loaded two iterations and the adjacency row one iteration before the row is staged, so no
-  // iteration waits for a load it issued.  check() gives the staged value: slot 40 carries
-  // NONE for a brick that is not computed (past the list, or out of range: flagged).
-  auto load_b = [&](unsigned long long n) -> unsigned { return (t < 81 && n < nlist) ? blist[n] : NONE; };
-  auto load_v = [&](unsigned b) -> unsigned { return (t < 81 && b < nbricks) ? adj[(size_t)b * 81 + t] : 0u; };
+  // Staging of list entry n's adjacency entries: thread t < nneed holds slot need[t].  check()
+  // gives the staged value: slot 40 carries NONE for a brick that is not computed (past the
+  // list, or out of range: flagged).
+  // (the last threads of the CTA: warp 0 issues the most copies)
+  const int nstage = (int)nneed, ts = NT4 - 1 - t;
+  const bool stager = ts < nstage;
+  const unsigned myslot = stager ? need[ts] : 0u;
+  const bool ctr = stager && myslot == 40u;
+  auto load_b = [&](unsigned long long n) -> unsigned { return (stager && n < nlist) ? blist[n] : NONE; };
+  auto load_v = [&](unsigned b) -> unsigned { return (stager && b < nbricks) ? adj[(size_t)b * 81 + myslot] : 0u; };
   auto check = [&](unsigned long long n, unsigned b, unsigned v) -> unsigned {
-    if (n >= nlist) return t == 40 ? NONE : 0u;
+    if (n >= nlist) return ctr ? NONE : 0u;
     if (b >= nbricks) {
-      if (t == 40) {
+      if (ctr) {
         atomicOr(err, FLAG_BOUNDS);
         return NONE;
       }
       return 0u;
     }
-    if ((long long)v >= in_chunks || (t == 40 && (long long)v >= out_chunks)) {
-      atomicOr(err, FLAG_BOUNDS);
-      return t == 40 ? NONE : 0u;
+    if ((long long)v >= in_chunks || (ctr && (long long)v >= out_chunks)) {
+      if (stager) atomicOr(err, FLAG_BOUNDS);
+      return ctr ? NONE : 0u;
     }
     return v;
   };
@@ -150,58 +186,57 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     const unsigned *nb = nbr[slot];
     if (nb[40] != NONE) {
       const unsigned base = (unsigned)__cvta_generic_to_shared(&tile[buf][0]);
-      // entries t, t + NT4, ... of the table (a compile-time count per thread)
-      constexpr int NPT = (NENT + NT4 - 1) / NT4;
-      const int ne = (int)nent;
+      const int a16 = (int)n16, ael = (int)nel;
+      // entries t, t + NT4, ... of each part of the table (compile-time counts per thread)
+      constexpr int NP16 = (G::ROWS * NSEG + NT4 - 1) / NT4, NPEL = (NTAB + NT4 - 1) / NT4;
 #pragma unroll
-      for (int m = 0; m < NPT; ++m) {
+      for (int m = 0; m < NP16; ++m) {
         const int e = t + NT4 * m;
-        if (e >= ne) break;
+        if (e >= a16) break;
         const unsigned w = plan[e];
-        const T *src = in + (size_t)nb[w & 127u] * in_step;
-        const unsigned dst = base + ((w >> 7) & 0x3FFFu) * (unsigned)sizeof(T);
-        const unsigned sw = srcw[e];
-        if ((w >> 30) == 1u) {
-          cp_async_elem<16>(dst, src + (sw & 255u));
-        } else {
+        cp_async_elem<16>(base + ((w >> 7) & 0x3FFFu) * (unsigned)sizeof(T), in + (size_t)nb[w & 127u] * in_step + (w >> 21));
+      }
 #pragma unroll
-          for (int q = 0; q < VE; ++q)
-            if ((w >> (21 + q)) & 1u) cp_async_elem<sizeof(T)>(dst + q * (unsigned)sizeof(T), src + ((sw >> (8 * q)) & 255u));
-        }
+      for (int m = 0; m < NPEL; ++m) {
+        const int e = t + NT4 * m;
+        if (e >= ael) break;
+        const unsigned w = plan[NTAB - 1 - e];
+        cp_async_elem<sizeof(T)>(base + ((w >> 7) & 0x3FFFu) * (unsigned)sizeof(T),
+                                 in + (size_t)nb[w & 127u] * in_step + (w >> 21));
       }
     }
     cp_async_commit4();
   };
   const unsigned long long n0 = blockIdx.x;
-  {
-    const unsigned b0 = load_b(n0), b1 = load_b(n0 + gs);
-    const unsigned a0 = check(n0, b0, load_v(b0)), a1 = check(n0 + gs, b1, load_v(b1));
-    if (t < 81) {
-      nbr[0][t] = a0;
-      nbr[1][t] = a1;
-    }
+  // bricks n0 .. n0 + (S-1) gs staged into slots 0 .. S-1
+#pragma unroll
+  for (int q = 0; q < S; ++q) {
+    const unsigned long long nq = n0 + q * gs;
+    const unsigned bq = load_b(nq);
+    const unsigned aq = check(nq, bq, load_v(bq));
+    if (stager) nbr[q][myslot] = aq;
   }
-  unsigned ba = load_b(n0 + 2 * gs);  // list entry n + 2 gs and its adjacency row
-  unsigned va = load_v(ba);
-  unsigned bb = load_b(n0 + 3 * gs);  // list entry n + 3 gs
-  __syncthreads();  // tables and the first two adjacency slots
-  issue(0, 0);
-  // this thread's output elements t and t + NT4: their tile positions and in-brick offsets (the
-  // layout's divisions by the fold, once per kernel instead of once per brick)
+  // in flight: list entries n0 + S gs (bA), + (S+1) gs (bB), + (S+2) gs (bC); adjacency of bA, bB
+  unsigned bA = load_b(n0 + S * gs), bB = load_b(n0 + (S + 1) * gs), bC = load_b(n0 + (S + 2) * gs);
+  unsigned vA = load_v(bA), vB = load_v(bB);
+  __syncthreads();  // the first S adjacency slots
+#pragma unroll
+  for (int q = 0; q + 1 < S; ++q) issue(q, q);
+  // this thread's output elements t and t + NT4: their tile positions and in-brick offsets
   static_assert(2 * NT4 == B * B * B * B, "two points per thread");
   int ctile[2], oofs[2];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int pt = t + NT4 * h;
     const int oi = pt % B, oj = (pt / B) % B, ok = (pt / (B * B)) % B, ol = pt / (B * B * B);
-    ctile[h] = (((ol + R) * E + (ok + R)) * E + (oj + R)) * EI + (oi + RP);
+    ctile[h] = G::toff(ol + R, ok + R, oj + R, oi) + C0;
     oofs[h] = L.offset(ol, ok, oj, oi);
   }
   // the tap list of a star of this radius fits MT entries: offsets held in registers for the
   // whole kernel (the loop over a runtime count read them from the parameters per tap)
-  int toffr[MT];
+  int toffr[CANON ? 1 : MT];
 #pragma unroll
-  for (int q = 0; q < MT; ++q) toffr[q] = q < tp.n ? tp.toff[q] : 0;
+  for (int q = 0; q < (CANON ? 1 : MT); ++q) toffr[q] = q < tp.n ? tp.toff[q] : 0;
   constexpr bool F64 = sizeof(AT) == 8;
   AT cr[MT];
 #pragma unroll
@@ -216,23 +251,47 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     if constexpr (F64) return fma(k, x, mz);
     else return k * x;
   };
-  int jb = 0;
-  for (unsigned long long n = n0; n < nlist; n += gs, ++jb) {
-    const int cur = jb % 3, nxt = (jb + 1) % 3, far = (jb + 2) % 3, buf = jb & 1;
-    __syncthreads();  // the previous brick's compute is done with tile[buf ^ 1] and slot far
-    issue(nxt, buf ^ 1);
-    const unsigned staged = check(n + 2 * gs, ba, va);
-    if (t < 81) nbr[far][t] = staged;
-    ba = bb;
-    va = load_v(bb);
-    bb = load_b(n + 4 * gs);
-    cp_async_wait4<1>();  // this thread's copies for brick n have landed
-    __syncthreads();      // ... and everybody else's
+  int sc = 0, sb = 0;  // slot and buffer of brick jb (jb mod NSLOT, jb mod S)
+  for (unsigned long long n = n0; n < nlist; n += gs) {
+    const int sl = sc + S - 1 - (sc + S - 1 >= NSLOT ? NSLOT : 0);  // brick jb + S - 1
+    const int bl = sb == 0 ? S - 1 : sb - 1;                        // its buffer, (jb + S - 1) mod S
+    const int sf = sc == 0 ? NSLOT - 1 : sc - 1;                    // brick jb + S: slot (jb - 1) mod NSLOT
+    cp_async_wait4<S - 2>();  // this thread's copies for brick jb have landed
+    // one barrier per brick: everybody's copies for brick jb have landed, and everybody is done
+    // with brick jb-1's compute (its buffer bl and slot sf) and has staged brick jb+S-1 (slot sl)
+    __syncthreads();
+    issue(sl, bl);
+    const unsigned staged = check(n + S * gs, bA, vA);
+    if (stager) nbr[sf][myslot] = staged;
+    bA = bB;
+    vA = vB;
+    bB = bC;
+    vB = load_v(bC);
+    bC = load_b(n + (S + 3) * gs);
+    const int cur = sc, buf = sb;
+    sc = sc + 1 == NSLOT ? 0 : sc + 1;
+    sb = sb + 1 == S ? 0 : sb + 1;
     const unsigned ob = nbr[cur][40];
     if (ob != NONE) {
       const T *c0 = tile[buf] + ctile[0], *c1 = tile[buf] + ctile[1];
       AT v0, v1;
-      if (tp.n <= MT) {
+      if constexpr (CANON) {
+        // the star of radius R in its canonical order: every tile offset a constant
+        const AT k0 = F64 ? cr[0] : coefq(0);
+        v0 = first(k0, c0[0]);
+        v1 = first(k0, c1[0]);
+#pragma unroll
+        for (int ax = 0; ax < 4; ++ax)
+#pragma unroll
+          for (int d = -R; d <= R; ++d) {
+            if (d == 0) continue;
+            const int q = 1 + 2 * R * ax + (d < 0 ? d + R : d + R - 1);
+            const int o = d * (ax == 0 ? E * G::Q : ax == 1 ? G::Q : ax == 2 ? G::P : 1);
+            const AT kq = F64 ? cr[q] : coefq(q);
+            v0 = fma(kq, c0[o], v0);
+            v1 = fma(kq, c1[o], v1);
+          }
+      } else if (tp.n <= MT) {
         // up to MT taps (a radius-R star): unrolled, the offsets and coefficients from
         // registers, the taps past n predicated off; the thread's two points side by side
         const AT k0 = F64 ? cr[0] : coefq(0);
@@ -265,11 +324,32 @@ template <typename T, typename AT, int R>
 static int launch4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
                    unsigned nlist, const Layout4 &L, Taps4 tp, const int (*offs)[4], int star, cudaStream_t s) {
   // persistent CTAs (each builds its copy table once): as many as fit on the GPU
-  typedef Tile4<T, R> G;
-  auto kern = sweep4_kernel<T, AT, R>;
-  constexpr size_t smem = G::SMEM;
-  for (int t = 0; t < tp.n; ++t)
-    tp.toff[t] = ((offs[t][0] * G::E + offs[t][1]) * G::E + offs[t][2]) * G::EI + offs[t][3];
+  typedef Tile4<T, R, false> G;  // the tile geometry (the table size depends on canon)
+  for (int t = 0; t < tp.n; ++t) tp.toff[t] = G::toff(offs[t][0], offs[t][1], offs[t][2], offs[t][3]);
+  // the star of radius R, each tap once: coefficients passed in the canonical order (centre,
+  // then along l, k, j, i the distances -R..-1, 1..R) and summed in that order
+  constexpr int MT = 8 * R + 1;
+  bool canon = star && tp.n == MT;
+  if (canon) {
+    double c[MT];
+    bool seen[MT] = {};
+    for (int t = 0; t < tp.n && canon; ++t) {
+      int ax = -1, d = 0;
+      for (int a = 0; a < 4; ++a)
+        if (offs[t][a]) ax = a, d = offs[t][a];
+      const int q = ax < 0 ? 0 : 1 + 2 * R * ax + (d < 0 ? d + R : d + R - 1);
+      if (seen[q]) canon = false;
+      seen[q] = true;
+      c[q] = tp.c[t];
+    }
+    if (canon)
+      for (int q = 0; q < MT; ++q) {
+        tp.c[q] = c[q];
+        tp.cf[q] = (float)c[q];
+      }
+  }
+  auto kern = canon ? sweep4_kernel<T, AT, R, true> : sweep4_kernel<T, AT, R, false>;
+  const size_t smem = canon ? Tile4<T, R, true>::SMEM : G::SMEM;
   const char *ibase = reinterpret_cast<const char *>(in->dat) + in->offset * sizeof(T);
   const int vec = reinterpret_cast<uintptr_t>(ibase) % 16 == 0 && (in->step * sizeof(T)) % 16 == 0;
   int *err = device_error_word();
@@ -306,6 +386,7 @@ int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const b
     L.f[d] = lay->fold[d];
     if (L.b[d] != 4) return fail(BK_ERR_UNSUPPORTED, "4-D sweeps take 4x4x4x4 bricks (weak/main-4d.cpp)");
     if (L.f[d] <= 0 || L.b[d] % L.f[d]) return fail(BK_ERR_ARG, "fold must divide the brick dims");
+    L.lf[d] = L.f[d] == 1 ? 0 : (L.f[d] == 2 ? 1 : 2);
   }
   if (!in->dat || !out->dat || in->chunks <= 0 || out->chunks <= 0) return fail(BK_ERR_ARG, "fields need storage");
   if (in->offset + 256 > in->step || out->offset + 256 > out->step)

@@ -70,6 +70,32 @@ def test_sweep4_fp32_and_radius2():
     assert np.abs(got32 - ref32).max() <= 1e-5 * np.abs(ref32).max()
 
 
+@pytest.mark.parametrize("dtype", [_abi.BK_F64, _abi.BK_F32])
+@pytest.mark.parametrize("fold", [(1, 1, 1, 1), (1, 1, 2, 4), (2, 1, 4, 1)])
+@pytest.mark.parametrize("radius", [1, 2])
+def test_sweep4_box_stencils_match_the_array_oracle(radius, fold, dtype):
+    """Box tap lists, for which every tile row and both i halos are gathered, against the array
+    loop: the full radius-1 box (81 taps) and 81 taps picked from the radius-2 box, on three
+    folds; FP32 storage against the oracle on the FP32-rounded input (1e-5 of the largest)."""
+    n = 8
+    S = n + 24
+    arr = stencils.uniform(6, S ** 4).reshape((S,) * 4)
+    box = [tuple(int(a) - radius for a in t) for t in np.ndindex(*(2 * radius + 1,) * 4)]
+    if len(box) > 81:
+        box = [box[q] for q in np.random.default_rng(5).choice(len(box), size=81, replace=False)]
+    st = stencils.Stencil(f"box{radius}", box, stencils.uniform01(7, len(box)))
+    lay = B4.Layout4(fold=fold)
+    if dtype == _abi.BK_F64:
+        ref = array4.array_sweep4(arr, st.taps, st.coeff, (12,) * 4, (n,) * 4)
+        ok, md = mixed_ok(run4(arr, st, n, lay=lay), ref)
+        assert ok, f"max |diff| {md}"
+    else:
+        a32 = arr.astype(np.float32).astype(np.float64)
+        ref32 = array4.array_sweep4(a32, st.taps, st.coeff, (12,) * 4, (n,) * 4)
+        got32 = run4(arr, st, n, dtype=dtype, lay=lay)
+        assert np.abs(got32 - ref32).max() <= 1e-5 * np.abs(ref32).max()
+
+
 def test_sweep4_rejects_bad_arguments_and_flags_bad_lists():
     st = B4.mpi9pt()
     buf = B.DeviceBuffer(64 * 512 * 8)
