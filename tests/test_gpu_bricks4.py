@@ -96,6 +96,34 @@ def test_sweep4_box_stencils_match_the_array_oracle(radius, fold, dtype):
         assert np.abs(got32 - ref32).max() <= 1e-5 * np.abs(ref32).max()
 
 
+@pytest.mark.parametrize("dtype", [_abi.BK_F64, _abi.BK_F32])
+def test_sweep4_partial_and_reordered_stars_match_the_array_oracle(dtype):
+    """Stars that are not exactly the full star of the kernel's radius take the tap-list path
+    (a partial star, one with a repeated tap); the full star listed in a shuffled order is
+    summed in the kernel's canonical order: all three against the array oracle."""
+    n = 8
+    S = n + 24
+    arr = stencils.uniform(8, S ** 4).reshape((S,) * 4)
+    full = [(0, 0, 0, 0)] + [tuple(d if a == ax else 0 for a in range(4)) for ax in range(4) for d in (1, -1)]
+    order = np.random.default_rng(9).permutation(len(full))
+    cases = [
+        ("partial", [(0, 0, 0, 0), (1, 0, 0, 0), (-1, 0, 0, 0), (0, 0, 0, 1)]),
+        ("repeated", [(0, 0, 0, 0), (0, 0, 1, 0), (0, 0, 1, 0), (0, -1, 0, 0), (0, 0, 0, -1)]),
+        ("shuffled", [full[q] for q in order]),
+    ]
+    for name, taps in cases:
+        st = stencils.Stencil(name, taps, stencils.uniform01(10, len(taps)))
+        if dtype == _abi.BK_F64:
+            ref = array4.array_sweep4(arr, st.taps, st.coeff, (12,) * 4, (n,) * 4)
+            ok, md = mixed_ok(run4(arr, st, n), ref)
+            assert ok, f"{name}: max |diff| {md}"
+        else:
+            a32 = arr.astype(np.float32).astype(np.float64)
+            ref32 = array4.array_sweep4(a32, st.taps, st.coeff, (12,) * 4, (n,) * 4)
+            got32 = run4(arr, st, n, dtype=dtype)
+            assert np.abs(got32 - ref32).max() <= 1e-5 * np.abs(ref32).max(), name
+
+
 def test_sweep4_rejects_bad_arguments_and_flags_bad_lists():
     st = B4.mpi9pt()
     buf = B.DeviceBuffer(64 * 512 * 8)
