@@ -156,7 +156,9 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     nneed = c;
   }
   __syncthreads();
-  const unsigned long long gs = gridDim.x;
+  // list positions in 32 bits: the host holds lists below 2^31 entries, so n + (S + 3) gs stays
+  // far below 2^32
+  const unsigned gs = gridDim.x;
   // Staging of list entry n's adjacency entries: thread t < nneed holds slot need[t].  check()
   // gives the staged value: slot 40 carries NONE for a brick that is not computed (past the
   // list, or out of range: flagged).
@@ -165,9 +167,9 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
   const bool stager = ts < nstage;
   const unsigned myslot = stager ? need[ts] : 0u;
   const bool ctr = stager && myslot == 40u;
-  auto load_b = [&](unsigned long long n) -> unsigned { return (stager && n < nlist) ? blist[n] : NONE; };
+  auto load_b = [&](unsigned n) -> unsigned { return (stager && n < nlist) ? blist[n] : NONE; };
   auto load_v = [&](unsigned b) -> unsigned { return (stager && b < nbricks) ? adj[(size_t)b * 81 + myslot] : 0u; };
-  auto check = [&](unsigned long long n, unsigned b, unsigned v) -> unsigned {
+  auto check = [&](unsigned n, unsigned b, unsigned v) -> unsigned {
     if (n >= nlist) return ctr ? NONE : 0u;
     if (b >= nbricks) {
       if (ctr) {
@@ -207,11 +209,11 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     }
     cp_async_commit4();
   };
-  const unsigned long long n0 = blockIdx.x;
+  const unsigned n0 = blockIdx.x;
   // bricks n0 .. n0 + (S-1) gs staged into slots 0 .. S-1
 #pragma unroll
   for (int q = 0; q < S; ++q) {
-    const unsigned long long nq = n0 + q * gs;
+    const unsigned nq = n0 + q * gs;
     const unsigned bq = load_b(nq);
     const unsigned aq = check(nq, bq, load_v(bq));
     if (stager) nbr[q][myslot] = aq;
@@ -252,7 +254,7 @@ sweep4_kernel(const unsigned *__restrict__ adj, unsigned nbricks, const T *__res
     else return k * x;
   };
   int sc = 0, sb = 0;  // slot and buffer of brick jb (jb mod NSLOT, jb mod S)
-  for (unsigned long long n = n0; n < nlist; n += gs) {
+  for (unsigned n = n0; n < nlist; n += gs) {
     const int sl = sc + S - 1 - (sc + S - 1 >= NSLOT ? NSLOT : 0);  // brick jb + S - 1
     const int bl = sb == 0 ? S - 1 : sb - 1;                        // its buffer, (jb + S - 1) mod S
     const int sf = sc == 0 ? NSLOT - 1 : sc - 1;                    // brick jb + S: slot (jb - 1) mod NSLOT
@@ -404,6 +406,7 @@ int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const b
   if (r > 2) return fail(BK_ERR_UNSUPPORTED, "4-D stencils of radius up to 2");
   if (nlist == 0) return BK_OK;
   if (!adj || !blist || nbricks == 0) return fail(BK_ERR_ARG, "adjacency, brick list and nbricks are required");
+  if (nlist >= (1u << 31)) return fail(BK_ERR_ARG, "4-D brick lists hold fewer than 2^31 entries");
   const int R = r <= 1 ? 1 : 2;
   Taps4 tp;
   tp.n = st->npoints;

@@ -202,8 +202,10 @@ typedef struct bk_stencil4 {
 } bk_stencil4;
 
 /* One 4-D sweep over the listed bricks: out = sum c_t * in(l+dl, k+dk, j+dj, i+di).  4x4x4x4
- * bricks, FP64 or FP32 storage (native arithmetic), radius up to 2.  Same field, list and
- * error conventions as bk_sweep. */
+ * bricks, FP64 or FP32 storage (native arithmetic), radius up to 2, lists of fewer than 2^31
+ * bricks.  Same field, list and error conventions as bk_sweep.  A tap list that is exactly the
+ * star of its radius is summed in the order centre, then along l, k, j, i the distances -R..-1,
+ * 1..R, whatever order it is listed in; any other tap list in its listed order. */
 int bk_sweep4(const unsigned *adj, unsigned nbricks, const bk_field *in, const bk_field *out, const unsigned *blist,
               unsigned nlist, const bk_stencil4 *st, const bk_layout4 *lay, void *stream);
 
