@@ -142,6 +142,20 @@ def test_in_and_out_fields_that_alias_are_rejected():
         assert got == want, _abi.lib().bk_last_error()
 
 
+def test_sweep4_list_length_is_checked_before_any_launch():
+    """4-D sweeps walk their list with 32-bit positions: a list of 2^31 or more bricks is
+    BK_ERR_ARG, reported before anything touches the device (the pointers here are never read)."""
+    from bricklib_gb300 import bricks4 as B4
+    f = _abi.bk_field
+    base = 1 << 20
+    st4 = B4.to_c_stencil4(B4.mpi9pt())
+    lay4 = B4.Layout4().to_c()
+    a, b = f(C.c_void_p(base), 100, 512, 0, _abi.BK_F64), f(C.c_void_p(base), 100, 512, 256, _abi.BK_F64)
+    fake = C.c_void_p(base)
+    got = _abi.lib().bk_sweep4(fake, 100, C.byref(a), C.byref(b), fake, 1 << 31, C.byref(st4), C.byref(lay4), None)
+    assert got == _abi.BK_ERR_ARG and b"2^31" in _abi.lib().bk_last_error()
+
+
 def test_stencil_errors_are_reported_not_raised_in_c():
     bad = stencils.custom("far", [(0, 0, 9)], [1.0])
     with pytest.raises(_abi.BkError) as e:
