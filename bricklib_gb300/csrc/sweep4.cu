@@ -1,12 +1,13 @@
 // Four-dimensional bricks (weak/main-4d.cpp): Brick<Dim<4,4,4,4>, Dim<fold>> with a runtime
-// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 128 threads: the
-// part of a brick's neighbourhood the stencil reads (centre and faces for a star, the whole
-// radius-R box otherwise) is gathered into shared memory by asynchronous copies while earlier
-// bricks are computed (two bricks in flight for radius 1), two outputs per thread.  The copies
-// follow a table the CTA builds once from the layout: one entry per 16-byte block of a tile
-// row's centre and one per i-halo side, a single 16-byte copy where the block's elements are
-// consecutive in their brick, else one copy per element.  Out-of-range list or adjacency
-// entries are clamped / skipped and raise the device error flag, as in the 3-D kernels.
+// tap list, e.g. the 9-point star of stencils/mpi9pt.py.  Persistent CTAs of 128 threads, two
+// outputs per thread: the part of a brick's neighbourhood the stencil reads (centre and faces for
+// a star, the whole radius-R box otherwise) is gathered into a shared-memory tile by asynchronous
+// copies while earlier bricks are computed (two bricks in flight for FP32 at radius 1, one
+// otherwise).  The copies follow a table the CTA builds once from the layout, one word per copy:
+// a 16-byte copy where a block of a tile row's centre (or a whole i halo) is consecutive and
+// aligned in its brick, else one copy per element.  Out-of-range list entries, and out-of-range
+// adjacency entries in the slots the tile reads, are clamped / skipped and raise the device error
+// flag, as in the 3-D kernels.
 #include "bk_common.cuh"
 
 namespace bk {
