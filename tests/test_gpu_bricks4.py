@@ -124,6 +124,26 @@ def test_sweep4_partial_and_reordered_stars_match_the_array_oracle(dtype):
             assert np.abs(got32 - ref32).max() <= 1e-5 * np.abs(ref32).max(), name
 
 
+@pytest.mark.parametrize("dtype", [_abi.BK_F64, _abi.BK_F32])
+def test_sweep4_mpi9pt_at_the_bench_size(dtype):
+    """mpi9pt over the 64^4 domain the 4-D bench line times (18^4 bricks with one ghost brick a
+    side, the default fold): every interior point against the array oracle (FP64: the mixed test
+    at 1e-12; FP32 storage: the oracle on the FP32-rounded input, 1e-5 of the largest)."""
+    n = 64
+    S = n + 8
+    arr = stencils.uniform(12, S ** 4).reshape((S,) * 4)
+    st = B4.mpi9pt()
+    if dtype == _abi.BK_F64:
+        ref = array4.array_sweep4(arr, st.taps, st.coeff, (4,) * 4, (n,) * 4)
+        ok, md = mixed_ok(run4(arr, st, n, ghost=4, pad=0), ref)
+        assert ok, f"max |diff| {md}"
+    else:
+        a32 = arr.astype(np.float32).astype(np.float64)
+        ref32 = array4.array_sweep4(a32, st.taps, st.coeff, (4,) * 4, (n,) * 4)
+        got32 = run4(arr, st, n, dtype=dtype, ghost=4, pad=0)
+        assert np.abs(got32 - ref32).max() <= 1e-5 * np.abs(ref32).max()
+
+
 def test_sweep4_rejects_bad_arguments_and_flags_bad_lists():
     st = B4.mpi9pt()
     buf = B.DeviceBuffer(64 * 512 * 8)
