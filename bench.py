@@ -724,8 +724,8 @@ def run_serving(args):
 
 def forms_record(args) -> dict:
     """The three forms in compact runs (about a minute together), for the default line: the
-    batched form (default bricks, no autotuning), 200 served jobs at 200 and 2000 jobs/s, and the
-    precision form's errors after 1 and 10 steps at 512^3."""
+    batched form (default bricks, no autotuning), 200 served jobs at 200 and 2000 jobs/s, the
+    precision form's errors after 1 and 10 steps at 512^3; and of the next rows the 4-D sweep."""
     import torch
     from bricklib_gb300 import _abi, precision, serving
     out = {}
@@ -746,7 +746,51 @@ def forms_record(args) -> dict:
                         "records": [{k: r[k] for k in ("stencil", "variant", "steps", "max_rel_err", "rms_rel_err")}
                                     for r in recs],
                         "seconds": round(time.perf_counter() - t, 1)}
+    t = time.perf_counter()
+    out["next"] = {"sweep4_mpi9pt": sweep4_record(10, 3), "seconds": None}
+    out["next"]["seconds"] = round(time.perf_counter() - t, 1)
     return out
+
+
+def sweep4_record(K: int, warmup: int) -> dict:
+    """The 4-D 9-point star (stencils/mpi9pt.py) on 64^4 points, 4^4 bricks with one ghost brick
+    per side, in and out interleaved in one storage (weak/main-4d.cpp's layout), FP64 and FP32
+    storage: CUDA events around K launches after `warmup`, on the current stream."""
+    import torch
+    from bricklib_gb300 import _abi, bricks as B, bricks4 as B4
+    from bricklib_gb300._abi import call
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    hbm, _ = peaks()
+    n4 = 64
+    gb4 = n4 // 4 + 2
+    grid4, adj4 = B4.init_grid([gb4] * 4)
+    adj_dev = B.DeviceBuffer(adj4.nbytes)
+    adj_dev.upload(np.ascontiguousarray(adj4))
+    g4 = grid4.reshape((gb4,) * 4)
+    inner = B.BrickList(np.ascontiguousarray(g4[1:-1, 1:-1, 1:-1, 1:-1].reshape(-1)))
+    st4 = B4.mpi9pt()
+    rec = {"points": n4 ** 4, "bricks": int(len(grid4)), "steps": K, "warmup": warmup}
+    for name, dt in (("f64", _abi.BK_F64), ("f32", _abi.BK_F32)):
+        s4 = B.BrickStorage.allocate_device(len(grid4), 512, dt)
+        call("bk_fill_uniform", C.c_void_p(s4.ptr), len(grid4) * 512, dt, 5, -1.0, 1.0, sp)
+        for _ in range(warmup):
+            B4.sweep4(adj_dev, len(grid4), s4, 0, 256, inner, st4, stream=sp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(K):
+            B4.sweep4(adj_dev, len(grid4), s4, 0, 256, inner, st4, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / K * 1e-3
+        nbytes = 2 * B.ELEM_SIZE[dt] * n4 ** 4
+        rec[name] = {"ms": round(sec * 1e3, 4), "gstencil_s": round(n4 ** 4 / sec / 1e9, 2),
+                     "gb_s": round(nbytes / sec / 1e9, 1), "hbm_frac": round(nbytes / sec / 1e9 / hbm, 4)}
+        del s4
+    if B.error_flags() != 0:
+        raise RuntimeError("4-D sweep raised device error flags")
+    return rec
 
 
 def run_next(args):
@@ -826,24 +870,7 @@ def run_next(args):
     out["decomp_exchange"]["regions"] = dec.nregions
     dec.close()
     del dst
-    # 4-D 9-point star on 64^4 points (4^4 bricks, one ghost brick per side)
-    n4 = 64
-    gb4 = n4 // 4 + 2
-    grid4, adj4 = B4.init_grid([gb4] * 4)
-    adj_dev = B.DeviceBuffer(adj4.nbytes)
-    adj_dev.upload(np.ascontiguousarray(adj4))
-    g4 = grid4.reshape((gb4,) * 4)
-    inner = B.BrickList(np.ascontiguousarray(g4[1:-1, 1:-1, 1:-1, 1:-1].reshape(-1)))
-    st4 = B4.mpi9pt()
-    out["sweep4_mpi9pt"] = {"points": n4 ** 4}
-    for name, dt in (("f64", f64), ("f32", _abi.BK_F32)):
-        s4 = B.BrickStorage.allocate_device(len(grid4), 512, dt)
-        call("bk_fill_uniform", C.c_void_p(s4.ptr), len(grid4) * 512, dt, 5, -1.0, 1.0, sp)
-        sec = timed(lambda: B4.sweep4(adj_dev, len(grid4), s4, 0, 256, inner, st4, stream=sp))
-        r = rate(2 * B.ELEM_SIZE[dt] * n4 ** 4, sec)
-        r["gstencil_s"] = round(n4 ** 4 / sec / 1e9, 2)
-        out["sweep4_mpi9pt"][name] = r
-        del s4
+    out["sweep4_mpi9pt"] = sweep4_record(K, args.warmup)
     assert B.error_flags() == 0
     if rank == 0:
         print(json.dumps(out), flush=True)
