@@ -725,7 +725,8 @@ def run_serving(args):
 def forms_record(args) -> dict:
     """The three forms in compact runs (about a minute together), for the default line: the
     batched form (default bricks, no autotuning), 200 served jobs at 200 and 2000 jobs/s, the
-    precision form's errors after 1 and 10 steps at 512^3; and of the next rows the 4-D sweep."""
+    precision form's errors after 1 and 10 steps at 512^3; and of the next rows the periodic ghost
+    fill at 512^3 and the 4-D sweep."""
     import torch
     from bricklib_gb300 import _abi, precision, serving
     out = {}
@@ -747,9 +748,43 @@ def forms_record(args) -> dict:
                                     for r in recs],
                         "seconds": round(time.perf_counter() - t, 1)}
     t = time.perf_counter()
-    out["next"] = {"sweep4_mpi9pt": sweep4_record(10, 3), "seconds": None}
+    out["next"] = {"ghost_fill_512": ghost_record(20, 3), "sweep4_mpi9pt": sweep4_record(10, 3), "seconds": None}
     out["next"]["seconds"] = round(time.perf_counter() - t, 1)
     return out
+
+
+def ghost_record(K: int, warmup: int) -> dict:
+    """The periodic ghost fill of the 512^3 FP64 domain with one ghost brick a side (66^3 bricks,
+    25,352 ghost bricks, each 4 KiB read from its periodic image and written): CUDA events
+    around K fills after `warmup`, on the current stream."""
+    import torch
+    from bricklib_gb300 import _abi, bricks as B
+    from bricklib_gb300._abi import call
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    hbm, _ = peaks()
+    gb = 512 // 8 + 2
+    grid, info = B.init_grid([gb] * 3)
+    st = B.BrickStorage.allocate_device(info.nbricks, 512, _abi.BK_F64)
+    call("bk_fill_uniform", C.c_void_p(st.ptr), info.nbricks * 512, _abi.BK_F64, 3, -1.0, 1.0, sp)
+    dinfo = B.movBrickInfo(info)
+    brick = B.Brick(dinfo, st, 0)
+    plan = B.GhostPlan.periodic(grid, (gb - 2,) * 3, (1, 1, 1))
+    for _ in range(warmup):
+        B.ghostFill(plan, brick, sp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        B.ghostFill(plan, brick, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / K * 1e-3
+    nbytes = 2 * plan.n * 512 * 8
+    if B.error_flags() != 0:
+        raise RuntimeError("ghost fill raised device error flags")
+    return {"ghost_bricks": plan.n, "steps": K, "warmup": warmup, "ms": round(sec * 1e3, 4),
+            "gb_s": round(nbytes / sec / 1e9, 1), "hbm_frac": round(nbytes / sec / 1e9 / hbm, 4)}
 
 
 def sweep4_record(K: int, warmup: int) -> dict:
