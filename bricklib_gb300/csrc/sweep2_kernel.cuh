@@ -134,13 +134,21 @@ __host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, in
 #define BK_CS_CHUNK 16
 #endif
 
+// resident two-warp CTAs per SM asked of the register allocator for the compensated FP32 / BF16
+// class-sum stream (0: none; at 6 the FP32 stream is held to 168 registers, spilling ~70 bytes:
+// GB300, cube125 at 512^3, 114.5 against 99.3 GStencil/s with no hint, BF16 109.0 / 110.7)
+#ifndef BK_CS_COMP_MINB
+#define BK_CS_COMP_MINB 6
+#endif
+
 #ifndef BK_PAIR_NB
 #define BK_PAIR_NB 1
 #endif
 constexpr int PAIR_NB = BK_PAIR_NB;
 
 // IST: the class-sum stream of the mirror-symmetric cubes (sym_cube_istream for FP64,
-// sym_cube_istream4 for 4- and 2-byte storage), one warp per 8x8x8 brick.
+// sym_cube_istream4 for 4- and 2-byte storage), one warp per 8x8x8 brick (two for the
+// compensated 4- and 2-byte stream, one row per thread).
 template <typename T, int BK, int BJ, int BI, int R, int FAM, int ACC, bool IST = false>
 struct Sweep2Cfg {
   static constexpr int ES = (int)sizeof(T);
@@ -178,8 +186,12 @@ struct Sweep2Cfg {
   // cube125 191 / 156; BF16 cube27 412 / 302, cube125 235 / 139).
   static constexpr bool PAIR = BK == 8 && BJ == 8 && BI == 8 && ACC == ACCM_NATIVE &&
                                (FAM == FAM_CUBESYM || FAM == FAM_CUBESYM_IJ || (FAM == FAM_CUBE && R == 1 && ES <= 4));
-  static constexpr bool WARP1 = PAIR || CS4;  // one warp per brick
-  static constexpr int TPB = WARP1 ? BJ * BI / 2 : BJ * BI;
+  static constexpr bool WARP1 = PAIR || CS4;  // one warp per brick (the compensated stream: two)
+  // rows of the brick per thread in the FP32 / BF16 class-sum stream: two in native arithmetic
+  // (one warp per brick), one under compensated accumulation (two warps per brick), whose Dot2
+  // state per row would otherwise cap the SM at 8 warps (255 registers)
+  static constexpr int CSROWS = CS4 && ACC == ACCM_COMP ? 1 : 2;
+  static constexpr int TPB = CS4 ? BK * BJ / CSROWS : WARP1 ? BJ * BI / 2 : BJ * BI;
   // vectors of the neighbourhood (per brick)
   static constexpr int NV_CENTRE = BK * BJ * (BI / VE);
   static constexpr int NV_KF = R * BJ * (BI / VE);   // one k face
@@ -206,9 +218,9 @@ struct Sweep2Cfg {
   static constexpr int COEFB = F64S ? ((F64Ops::NHEAD + NCOEF) * 8 + 15) / 16 * 16 : 0;
   static constexpr int SMEM = NB * PER_BRICK + COEFB;
   // resident CTAs asked of the register allocator: the native FP32 / BF16 class-sum stream
-  // (one warp per CTA) at <= 170 registers fits three warps per scheduler (12 per SM), which
-  // its shared memory also allows
-  static constexpr int MINB = CS4 && ACC == ACCM_NATIVE ? 12 : 0;
+  // (one warp per CTA) at <= 170 registers fits three warps per scheduler (12 per SM), which its
+  // shared memory also allows; the compensated stream (two warps per CTA): BK_CS_COMP_MINB
+  static constexpr int MINB = CS4 ? (ACC == ACCM_NATIVE ? 12 : BK_CS_COMP_MINB) : 0;
 };
 
 // Tile coordinates (kk, jj, ii) of plan vector g for the star / cube neighbourhood.
@@ -659,22 +671,23 @@ __device__ __forceinline__ void st_quad(__nv_bfloat16 *g, const __nv_bfloat16 *t
 
 // W of the current and previous 4-column groups of a stream, per row o, a = 0..R and column
 // pair; with the Dot2 error terms of each W under compensated accumulation.
-template <int R, bool COMP>
+template <int R, bool COMP, int NO>
 struct CsWin {
-  float2 p[2][R + 1][2], c[2][R + 1][2];
-  float2 ep[COMP ? 2 : 1][R + 1][2], ec[COMP ? 2 : 1][R + 1][2];
+  float2 p[NO][R + 1][2], c[NO][R + 1][2];
+  float2 ep[COMP ? NO : 1][R + 1][2], ec[COMP ? NO : 1][R + 1][2];
 };
 
-// W_a (and errors) of the four tile columns c0 .. c0 + 3 for both rows of this lane.
-// base: tile row j of plane k0 (brick-local (k0 - R, j - R)); rows j .. j + 2R are read.
-template <typename C, typename T, int R, bool KJ, bool COMP>
+// W_a (and errors) of the four tile columns c0 .. c0 + 3 for the NO rows (k0 .. k0 + NO - 1, j)
+// of this thread.  base: tile row j of plane k0 (brick-local (k0 - R, j - R)); rows j .. j + 2R
+// are read.
+template <typename C, typename T, int R, bool KJ, bool COMP, int NO>
 __device__ __forceinline__ void cs_group(const T *base, const int j, const int c0, const Taps &tp,
-                                         float2 (&W)[2][R + 1][2], float2 (&E)[COMP ? 2 : 1][R + 1][2]) {
+                                         float2 (&W)[NO][R + 1][2], float2 (&E)[COMP ? NO : 1][R + 1][2]) {
   constexpr int SK = C::EJ * C::EI, SJ = C::EI;
-  float2 Q[2][R + 1][R + 1][2];  // [o][c][b][pair]
+  float2 Q[NO][R + 1][R + 1][2];  // [o][c][b][pair]
   const unsigned sb = smem_u32(base);
 #pragma unroll
-  for (int q = 0; q < 2 * R + 2; ++q) {  // tile plane k0 + q: brick-local plane k0 - R + q
+  for (int q = 0; q < 2 * R + NO; ++q) {  // tile plane k0 + q: brick-local plane k0 - R + q
     float2 v[2 * R + 1][2];
 #pragma unroll
     for (int rr = 0; rr <= 2 * R; ++rr)
@@ -688,7 +701,7 @@ __device__ __forceinline__ void cs_group(const T *base, const int j, const int c
       for (int b = 1; b <= R; ++b) H[b][h] = __fadd2_rn(v[R - b][h], v[R + b][h]);
     }
 #pragma unroll
-    for (int o = 0; o < 2; ++o) {
+    for (int o = 0; o < NO; ++o) {
       const int dk = q - R - o;  // offset of this plane from row k0 + o
       if (dk < -R || dk > R) continue;
       const int c = dk < 0 ? -dk : dk;
@@ -700,7 +713,7 @@ __device__ __forceinline__ void cs_group(const T *base, const int j, const int c
     }
   }
 #pragma unroll
-  for (int o = 0; o < 2; ++o) {
+  for (int o = 0; o < NO; ++o) {
     if constexpr (KJ) {
 #pragma unroll
       for (int c = 1; c <= R; ++c)
@@ -754,34 +767,34 @@ __device__ __forceinline__ float cs_at(const float2 (&P)[NO][R + 1][2], const fl
   return (m & 1) ? v.y : v.x;
 }
 
-// Outputs of the current group's four columns c0 .. c0 + 3 for both rows, parked in the tile at
-// their own input positions (park: tile row prow = j + R of plane k0 + R), one vector store per
-// row (the four columns are one 16-byte unit of the row, also under the FP32 swizzle; the eight
-// lanes of a quarter warp hit distinct banks).
-template <typename C, typename T, int R, bool COMP>
-__device__ __forceinline__ void cs_out(T *park, const int prow, const int c0, const CsWin<R, COMP> &S,
-                                       const float2 (&Wn)[2][R + 1][2], const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
+// Outputs of the current group's four columns c0 .. c0 + 3 for the thread's NO rows, parked in
+// the tile at their own input positions (park: tile row prow = j + R of plane k0 + R), one
+// vector store per row (the four columns are one 16-byte unit of the row, also under the FP32
+// swizzle; the eight lanes of a quarter warp hit distinct banks).
+template <typename C, typename T, int R, bool COMP, int NO>
+__device__ __forceinline__ void cs_out(T *park, const int prow, const int c0, const CsWin<R, COMP, NO> &S,
+                                       const float2 (&Wn)[NO][R + 1][2], const float2 (&En)[COMP ? NO : 1][R + 1][2]) {
   constexpr int SK = C::EJ * C::EI;
   static_assert(C::SWZ || C::EI % 4 == 0, "four parked columns stay in one aligned unit");
   const unsigned pb = smem_u32(park + C::col(prow, c0));
 #pragma unroll
-  for (int o = 0; o < 2; ++o) {
+  for (int o = 0; o < NO; ++o) {
     float q[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       float v;
       if constexpr (!COMP) {
-        v = cs_at<R, 2>(S.p, S.c, Wn, o, 0, t);
+        v = cs_at<R, NO>(S.p, S.c, Wn, o, 0, t);
 #pragma unroll
-        for (int a = 1; a <= R; ++a) v += cs_at<R, 2>(S.p, S.c, Wn, o, a, t - a) + cs_at<R, 2>(S.p, S.c, Wn, o, a, t + a);
+        for (int a = 1; a <= R; ++a) v += cs_at<R, NO>(S.p, S.c, Wn, o, a, t - a) + cs_at<R, NO>(S.p, S.c, Wn, o, a, t + a);
       } else {
-        float sm = cs_at<R, 2>(S.p, S.c, Wn, o, 0, t), cm = 0.f;
-        float es = cs_at<R, 2>(S.ep, S.ec, En, o, 0, t);
+        float sm = cs_at<R, NO>(S.p, S.c, Wn, o, 0, t), cm = 0.f;
+        float es = cs_at<R, NO>(S.ep, S.ec, En, o, 0, t);
 #pragma unroll
         for (int a = 1; a <= R; ++a) {
-          neumaier(sm, cm, cs_at<R, 2>(S.p, S.c, Wn, o, a, t - a));
-          neumaier(sm, cm, cs_at<R, 2>(S.p, S.c, Wn, o, a, t + a));
-          es += cs_at<R, 2>(S.ep, S.ec, En, o, a, t - a) + cs_at<R, 2>(S.ep, S.ec, En, o, a, t + a);
+          neumaier(sm, cm, cs_at<R, NO>(S.p, S.c, Wn, o, a, t - a));
+          neumaier(sm, cm, cs_at<R, NO>(S.p, S.c, Wn, o, a, t + a));
+          es += cs_at<R, NO>(S.ep, S.ec, En, o, a, t - a) + cs_at<R, NO>(S.ep, S.ec, En, o, a, t + a);
         }
         v = sm + (cm + es);
       }
@@ -791,11 +804,11 @@ __device__ __forceinline__ void cs_out(T *park, const int prow, const int c0, co
   }
 }
 
-template <int R, bool COMP>
-__device__ __forceinline__ void cs_shift(CsWin<R, COMP> &S, const float2 (&Wn)[2][R + 1][2],
-                                         const float2 (&En)[COMP ? 2 : 1][R + 1][2]) {
+template <int R, bool COMP, int NO>
+__device__ __forceinline__ void cs_shift(CsWin<R, COMP, NO> &S, const float2 (&Wn)[NO][R + 1][2],
+                                         const float2 (&En)[COMP ? NO : 1][R + 1][2]) {
 #pragma unroll
-  for (int o = 0; o < 2; ++o)
+  for (int o = 0; o < NO; ++o)
 #pragma unroll
     for (int a = 0; a <= R; ++a)
 #pragma unroll
@@ -812,39 +825,46 @@ __device__ __forceinline__ void cs_shift(CsWin<R, COMP> &S, const float2 (&Wn)[2
 // One brick of the stream: its eight output columns (groups at tile columns RP and RP + 4), the
 // W of groups RP - 4 and RP computed here unless the stream continues (cont), then the brick
 // leaves in whole-warp stores (16 / 8 bytes per lane) when the output brick is aligned for them.
+// A thread (lane of the brick's TPB threads) owns rows (k0 .. k0 + NO - 1, j); with two warps per
+// brick the syncs around the parking are block barriers.
 template <typename C, typename T, int R, bool KJ, bool COMP>
-__device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, const Taps &tp, CsWin<R, COMP> &S,
-                                                  const bool cont) {
-  constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP;
+__device__ __forceinline__ void sym_cube_istream4(T *rt, T *ob, const int lane, const Taps &tp,
+                                                  CsWin<R, COMP, C::CSROWS> &S, const bool cont) {
+  constexpr int SK = C::EJ * C::EI, SJ = C::EI, RP = C::RP, NO = C::CSROWS, TPB = C::TPB;
   static_assert(R == 1 || R == 2, "cube radius");
   static_assert(RP >= 4 && C::NEED >= RP + 12, "the four column groups of a brick fit the tile row");
-  const int k0 = 2 * (lane >> 3), j = lane & 7;
+  static_assert(TPB * NO == 64 && (TPB == 32 || TPB == 64), "the brick's 64 rows over its threads");
+  auto sync = [] {
+    if constexpr (TPB == 32) __syncwarp();
+    else __syncthreads();
+  };
+  const int k0 = NO * (lane >> 3), j = lane & 7;
   const T *base = rt + k0 * SK + j * SJ;
   T *park = rt + (k0 + R) * SK + (j + R) * SJ;
-  float2 Wn[2][R + 1][2], En[COMP ? 2 : 1][R + 1][2];
+  float2 Wn[NO][R + 1][2], En[COMP ? NO : 1][R + 1][2];
   if (!cont) {
-    cs_group<C, T, R, KJ, COMP>(base, j, RP - 4, tp, S.p, S.ep);
-    cs_group<C, T, R, KJ, COMP>(base, j, RP, tp, S.c, S.ec);
+    cs_group<C, T, R, KJ, COMP, NO>(base, j, RP - 4, tp, S.p, S.ep);
+    cs_group<C, T, R, KJ, COMP, NO>(base, j, RP, tp, S.c, S.ec);
   }
-  cs_group<C, T, R, KJ, COMP>(base, j, RP + 4, tp, Wn, En);
-  __syncwarp();  // every lane is past its reads of columns RP .. RP + 7
-  cs_out<C, T, R, COMP>(park, j + R, RP, S, Wn, En);
-  cs_shift<R, COMP>(S, Wn, En);
-  cs_group<C, T, R, KJ, COMP>(base, j, RP + 8, tp, Wn, En);  // the i-hi columns: never parked over
-  cs_out<C, T, R, COMP>(park, j + R, RP + 4, S, Wn, En);
-  cs_shift<R, COMP>(S, Wn, En);
-  __syncwarp();  // the parked outputs of every lane are in the tile
+  cs_group<C, T, R, KJ, COMP, NO>(base, j, RP + 4, tp, Wn, En);
+  sync();  // every thread is past its reads of columns RP .. RP + 7
+  cs_out<C, T, R, COMP, NO>(park, j + R, RP, S, Wn, En);
+  cs_shift<R, COMP, NO>(S, Wn, En);
+  cs_group<C, T, R, KJ, COMP, NO>(base, j, RP + 8, tp, Wn, En);  // the i-hi columns: never parked over
+  cs_out<C, T, R, COMP, NO>(park, j + R, RP + 4, S, Wn, En);
+  cs_shift<R, COMP, NO>(S, Wn, En);
+  sync();  // the parked outputs of every thread are in the tile
   constexpr int AL = 4 * (int)sizeof(T);
   if ((reinterpret_cast<uintptr_t>(ob) & (AL - 1)) == 0) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = q * 128 + 4 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
+    for (int q = 0; q < 512 / (4 * TPB); ++q) {
+      const int e = q * 4 * TPB + 4 * lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
       st_quad(ob + e, rt + (k + R) * SK + (jj + R) * SJ + C::col(jj + R, RP + i));
     }
   } else {
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int e = q * 32 + lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
+    for (int q = 0; q < 512 / TPB; ++q) {
+      const int e = q * TPB + lane, k = e >> 6, jj = (e >> 3) & 7, i = e & 7;
       ob[e] = rt[(k + R) * SK + (jj + R) * SJ + C::col(jj + R, RP + i)];
     }
   }
@@ -1298,12 +1318,14 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   // issue the asynchronous gather of the group staged in nbrs[ns] into raw buffer buf
   // Whether the stream continues from the group whose adjacency is in nbrs[prev] into the group
   // in nbrs[ns]: both ran, and the latter's i-lo and centre columns of neighbours are the
-  // former's centre and i-hi columns (warp-uniform; lanes 0..17 check one slot pair each).
+  // former's centre and i-hi columns (lanes 0..17 of every warp check one slot pair each, so
+  // all warps of a brick reach the same answer).
   auto continues = [&](int prev, int ns) -> bool {
     const unsigned *nb = nbrs + ns * 36, *pv = nbrs + prev * 36;
     bool same = true;
-    if (lt < 18) {
-      const int s9 = lt < 9 ? lt : lt - 9, sh = lt < 9 ? 0 : 1;
+    const int wl = lt & 31;
+    if (wl < 18) {
+      const int s9 = wl < 9 ? wl : wl - 9, sh = wl < 9 ? 0 : 1;
       const int base = (s9 / 3) * 9 + (s9 % 3) * 3;  // (dk, dj) = (s9 / 3 - 1, s9 % 3 - 1), di = -1
       same = nb[base + sh] == pv[base + sh + 1];
     }
@@ -1362,7 +1384,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
   // i-streaming: W of the last 2R columns of the previous brick (sym_cube_istream), or of the
   // last two 4-column groups (sym_cube_istream4)
   double W[IST && C::ES == 8 ? 2 : 1][IST && C::ES == 8 ? R + 1 : 1][IST && C::ES == 8 ? 2 * R + 1 : 1];
-  CsWin<R, ACC == ACCM_COMP> S4;
+  CsWin<R, ACC == ACCM_COMP, C::CSROWS> S4;
 
   for (int it = 0; grp < gend; grp = w2.g, w2 = w3, w3 = advance(w3), ++it) {
     const int cur = it & 1, nxt = cur ^ 1;
@@ -1394,7 +1416,7 @@ sweep2_kernel(const SweepArgs a, const Taps tp) {
         T *out = reinterpret_cast<T *>(*reinterpret_cast<const unsigned long long *>(nbr + 30));
         const size_t ostep = *reinterpret_cast<const unsigned long long *>(nbr + 34);
         T *ob = out + (size_t)nbr[13] * ostep;
-        T *tile = const_cast<T *>(rt);  // this warp's buffer until the next barrier
+        T *tile = const_cast<T *>(rt);  // this brick's buffer until the next barrier
         if constexpr (C::ES == 8) {
           if (tp.kj) sym_cube_istream<C, R, true>(tile, ob, lt, tp, W, cont);
           else sym_cube_istream<C, R, false>(tile, ob, lt, tp, W, cont);
