@@ -135,10 +135,11 @@ __host__ __device__ constexpr int conflict_free_row(int need, int bi, int es, in
 #endif
 
 // resident two-warp CTAs per SM asked of the register allocator for the compensated FP32 / BF16
-// class-sum stream (0: none; at 6 the FP32 stream is held to 168 registers, spilling ~70 bytes:
-// GB300, cube125 at 512^3, 114.5 against 99.3 GStencil/s with no hint, BF16 109.0 / 110.7)
+// class-sum stream (0: none).  GB300, cube125 at 512^3, FP32 / BF16 GStencil/s: none (182 / 146
+// registers) 99.3 / 110.7; 6 (168, some spilled) 114.5 / 109.0; 8 (128, 50-80 bytes spilled)
+// 119.8 / 112.8; 10 (96, 100-150 bytes spilled) 114.1 / 109.1
 #ifndef BK_CS_COMP_MINB
-#define BK_CS_COMP_MINB 6
+#define BK_CS_COMP_MINB 8
 #endif
 
 #ifndef BK_PAIR_NB
